@@ -1,0 +1,352 @@
+"""Benchmark of the GB300 CSR SpGEMM library (one JSON line on stdout, rank 0).
+
+Default workload: C = A*A in FP64 on the 1,000,000-row synthetic web-like power-law graph
+(the configuration the headline throughput is quoted on).  One step = one complete
+SpGEMM (row classification, symbolic phase, row_ptr scan, C allocation from the
+handle's pool, numeric phase) through the C ABI call ops_spgemm, inputs resident in HBM.
+`value` = 2 * intermediate products / mean device time per step (GFLOPS).
+`e2e`   = the same metric through the same call with host buffers: each step copies A
+          from pinned host memory, multiplies, and copies all of C back.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--workload web|laplacian|stencil27|stencil27_f32]
+
+--impl reference times the CPU baseline (OpenMP row-wise hash Gustavson, the oracle's
+port; OpSparse itself has no CPU SpGEMM) on the same workload and prints its line.
+Under torchrun each rank runs its own replica (weak scaling) and rank 0 prints.
+"""
+from __future__ import annotations
+
+import argparse
+import csv
+import ctypes as C
+import io
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "SpGEMM GFLOPS & %HBM peak; batched and fwd+bwd vs plain at matched tol"
+L2_FLUSH_BYTES = 256 << 20
+FALLBACK_HBM_GBS = 6800.0
+
+
+# ----------------------------------------------------------------------------- inputs
+def make_workload(name: str):
+    from opsparse_gb300 import gen
+
+    if name == "web":
+        rpt, col, val = gen.web_powerlaw()
+        desc = {"workload": "web_powerlaw_1M", "rows": 1_000_000, "row_len_exponent": 2.1, "row_len_max": 4700,
+                "local_window": 512, "global_zipf_s": 1.0, "values": "U(0,1)", "op": "C=A*A", "seed": gen.SEED}
+        dt = "f64"
+    elif name == "laplacian":
+        rpt, col, val = gen.laplacian2d(128)
+        desc = {"workload": "laplacian2d_128x128", "rows": 16384, "op": "C=A*A"}
+        dt = "f64"
+    elif name in ("stencil27", "stencil27_f32"):
+        rpt, col, val = gen.stencil27(80)
+        desc = {"workload": "stencil27_80^3", "rows": 512000, "values": "N(0,1)", "op": "C=A*A", "seed": gen.SEED}
+        dt = "f32" if name.endswith("f32") else "f64"
+    else:
+        raise SystemExit(f"unknown workload {name}")
+    n = len(rpt) - 1
+    if dt == "f32":
+        val = val.astype(np.float32)
+    return desc, dt, (rpt, col, val), n
+
+
+def bytes_alg(M, K, nnz_a, nnz_b, nnz_c, s):
+    sym = 4 * (M + 1) + 4 * nnz_a + 4 * (K + 1) + 4 * nnz_b + 4 * M
+    num = 4 * (M + 1) + (4 + s) * nnz_a + 4 * (K + 1) + (4 + s) * nnz_b + 4 * (M + 1) + (4 + s) * nnz_c
+    return sym + num
+
+
+def measured_peak():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        try:
+            return float(json.loads(p.read_text())["hbm_gbs"]), "measured"
+        except Exception:
+            pass
+    return FALLBACK_HBM_GBS, "fallback"
+
+
+# ----------------------------------------------------------------------------- clocks
+class ClockSampler:
+    """nvidia-smi sampling of SM clock and throttle reasons during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        self.out = ""
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.out, _ = self.proc.communicate(timeout=5)
+            except Exception:
+                self.proc.kill()
+                self.out = ""
+
+    def summary(self):
+        rows = [r for r in csv.reader(io.StringIO(self.out or "")) if len(r) >= 9]
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+
+        def f(x):
+            try:
+                return float(x)
+            except ValueError:
+                return None
+
+        sm = [f(r[1]) for r in rows if f(r[1]) is not None]
+        mx = [f(r[2]) for r in rows if f(r[2]) is not None]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].strip().lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+# ----------------------------------------------------------------------------- CPU side
+def cpu_baseline(data, n, steps=3):
+    import oracle
+
+    rpt, col, val = data
+    val64 = np.asarray(val, dtype=np.float64)
+    oracle.omp_spgemm(rpt, col, val64, rpt, col, val64)  # warm-up
+    ts = []
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        oracle.omp_spgemm(rpt, col, val64, rpt, col, val64)
+        ts.append(time.perf_counter() - t0)
+    return statistics.median(ts), oracle.num_threads()
+
+
+def run_reference(args, desc, dt, data, n, rank, world):
+    if rank != 0:
+        return
+    import oracle
+
+    P = int(oracle.flop(data[0], data[1], data[0])[0])
+    rpt, col, val = data
+    val64 = np.asarray(val, dtype=np.float64)
+    for _ in range(max(0, args.warmup)):
+        oracle.omp_spgemm(rpt, col, val64, rpt, col, val64)
+    ts = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        oracle.omp_spgemm(rpt, col, val64, rpt, col, val64)
+        ts.append(time.perf_counter() - t0)
+    t = statistics.mean(ts)
+    gf = 2.0 * P / t / 1e9
+    cores = oracle.num_threads()
+    line = {"metric": METRIC, "value": gf, "unit": "GFLOPS", "impl": "reference", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": desc,
+            "cpu_baseline": {"value": gf, "unit": "GFLOPS", "cores": cores, "kind": "port",
+                             "sample": f"full workload, {args.steps} runs, FP64, OpenMP row-wise hash Gustavson "
+                                       f"(OpSparse ships no CPU SpGEMM; this is the oracle's port)"},
+            "e2e": {"value": gf, "unit": "GFLOPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ----------------------------------------------------------------------------- GPU side
+def run_ours(args, desc, dt, data, n, rank, world, local_rank):
+    import torch
+
+    import opsparse_gb300 as ops
+    from opsparse_gb300 import capi
+
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    tdt = torch.float64 if dt == "f64" else torch.float32
+    s = 8 if dt == "f64" else 4
+    rpt, col, val = data
+    A = ops.csr_to_device(rpt, col, val, n, n, dtype=tdt, device=str(dev))
+    lib = capi.load()
+    h = ops.Handle()
+    stream = torch.cuda.current_stream()
+    st = C.c_void_p(stream.cuda_stream)
+    code = capi.OPS_F64 if dt == "f64" else capi.OPS_F32
+    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device=dev)
+    ap = A.ptrs()
+
+    def step():
+        rp, cp, vp = C.c_void_p(), C.c_void_p(), C.c_void_p()
+        nnz = C.c_int64(0)
+        capi.check(lib.ops_spgemm(h.h, code, n, n, n, ap[0], ap[1], ap[2], A.nnz, ap[0], ap[1], ap[2], A.nnz,
+                                  C.byref(rp), C.byref(cp), C.byref(vp), C.byref(nnz), st), h.h)
+        return rp, cp, vp, int(nnz.value)
+
+    def release(ptrs):
+        for p in ptrs[:3]:
+            lib.ops_free(p, st)
+
+    # untimed warm-up; also collect phase and per-class kernel times
+    for _ in range(max(args.warmup, 3)):
+        release(step())
+    h.set_timing(2)
+    out = step()
+    nnz_c = out[3]
+    phases = h.timings()
+    release(out)
+    h.set_timing(0)
+    P = int(phases["flop"])
+
+    # timed region: K steps, L2 flushed between steps outside the events
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    launches = 0
+    with ClockSampler(local_rank) as clk:
+        for i in range(args.steps):
+            flush.zero_()
+            ev[i][0].record(stream)
+            out = step()
+            ev[i][1].record(stream)
+            launches += h.timings()["launches"]
+            release(out)
+        torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    t_ms = float(np.mean(step_ms))
+    if world > 1:
+        tt = torch.tensor([t_ms], dtype=torch.float64, device=dev)
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        t_ms = float(tt.item())
+    gflops = world * 2.0 * P / (t_ms * 1e-3) / 1e9
+
+    # end to end through the same call with host buffers
+    pin = [torch.as_tensor(x).pin_memory() for x in (rpt, col, val)]
+    d_in = [torch.empty_like(x, device=dev) for x in pin]
+    h_out = [torch.empty(n + 1, dtype=torch.int32).pin_memory(), torch.empty(max(nnz_c, 1), dtype=torch.int32).pin_memory(),
+             torch.empty(max(nnz_c, 1), dtype=tdt).pin_memory()]
+    h2d = sum(x.numel() * x.element_size() for x in pin)
+    d2h = (n + 1) * 4 + nnz_c * (4 + s)
+    e2e_ms = []
+    for i in range(args.warmup + args.steps):
+        flush.zero_()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for d, p in zip(d_in, pin):
+            d.copy_(p, non_blocking=True)
+        rp2, cp2, vp2 = C.c_void_p(), C.c_void_p(), C.c_void_p()
+        nnz = C.c_int64(0)
+        capi.check(lib.ops_spgemm(h.h, code, n, n, n, d_in[0].data_ptr(), d_in[1].data_ptr(), d_in[2].data_ptr(),
+                                  A.nnz, d_in[0].data_ptr(), d_in[1].data_ptr(), d_in[2].data_ptr(), A.nnz,
+                                  C.byref(rp2), C.byref(cp2), C.byref(vp2), C.byref(nnz), st), h.h)
+        vstr = "<f8" if dt == "f64" else "<f4"
+        for hb, dp, cnt, ts in ((h_out[0], rp2, n + 1, "<i4"), (h_out[1], cp2, nnz_c, "<i4"),
+                                (h_out[2], vp2, nnz_c, vstr)):
+            dv = torch.as_tensor(ops._DevArray(dp.value, cnt, ts), device=dev)
+            hb[:cnt].copy_(dv, non_blocking=True)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        release((rp2, cp2, vp2))
+        if i >= args.warmup:
+            e2e_ms.append(e0.elapsed_time(e1))
+    e2e_t = float(np.mean(e2e_ms))
+    if world > 1:
+        tt = torch.tensor([e2e_t], dtype=torch.float64, device=dev)
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        e2e_t = float(tt.item())
+    e2e_gf = world * 2.0 * P / (e2e_t * 1e-3) / 1e9
+
+    if rank != 0:
+        return
+    peak, peak_kind = measured_peak()
+    nnz_a = len(col)
+    balg = bytes_alg(n, n, nnz_a, nnz_a, nnz_c, s)
+    achieved = balg / (t_ms * 1e-3) / 1e9
+    kms = phases["kernel_ms"]
+    names = ["R8", "R16", "R32", "W", "T", "D"]
+    per_kernel = {f"{ph}_{names[c]}": round(kms[i][c], 4) for i, ph in enumerate(("symbolic", "numeric"))
+                  for c in range(6) if kms[i][c] > 0}
+    line = {
+        "metric": METRIC, "value": gflops, "unit": "GFLOPS", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": t_ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": dt, "data": "synthetic (seeded stand-in for the SuiteSparse inputs)",
+        "config": dict(desc, l2="flushed between steps (256 MiB write outside the timed events)",
+                       products=P, nnz_a=nnz_a, nnz_c=nnz_c, parallelism=f"replica x{world}"),
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": None, "kernel": "whole SpGEMM pipeline (all launches of one C=A*B)",
+                     "algorithmic_bytes": balg, "peak_kind": peak_kind},
+        "phases_ms": {k: round(phases[k] * 1e3, 4) for k in ("symbolic_binning", "symbolic", "prefix", "allocate",
+                                                             "numeric", "total")},
+        "kernels_ms": per_kernel,
+        "class_rows": dict(zip(names, phases["class_rows"])),
+        "e2e": {"value": e2e_gf, "unit": "GFLOPS", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "ms_per_step": e2e_t},
+        "gpu_launches": launches,
+        "clocks": clk.summary(),
+    }
+    if args.cpu_baseline and world == 1:
+        t_cpu, cores = cpu_baseline(data, n)
+        line["cpu_baseline"] = {"value": 2.0 * P / t_cpu / 1e9, "unit": "GFLOPS", "cores": cores, "kind": "port",
+                                "sample": "full workload, median of 3 runs after 1 warm-up, FP64, OpenMP row-wise "
+                                          "hash Gustavson on the host cores"}
+    h.close()
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="web", choices=["web", "laplacian", "stencil27", "stencil27_f32"])
+    ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        if torch.cuda.is_available():
+            torch.cuda.set_device(local_rank)
+        dist.init_process_group(backend=backend)
+    desc, dt, data, n = make_workload(args.workload)
+    if args.impl == "reference":
+        run_reference(args, desc, dt, data, n, rank, world)
+    else:
+        run_ours(args, desc, dt, data, n, rank, world, local_rank)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

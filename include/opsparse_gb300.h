@@ -1,0 +1,139 @@
+/*
+ * opsparse_gb300.h — C ABI of the GB300 CSR SpGEMM library (libopsparse_gb300.so).
+ *
+ * Plain pointers and sizes only.  Every matrix argument is a CSR triple of DEVICE
+ * pointers: row_ptr (rows+1 int32), col_idx (nnz int32, ascending and unique within each
+ * row) and values (nnz elements of the call's value type).  Every function returns an
+ * ops_status (0 = success) and never throws.  Calls on one handle must not overlap;
+ * use one handle per host thread.
+ *
+ * Correspondence with OpSparse's C++ API (paths relative to its source tree):
+ *   ops_spgemm            <- opsparse_spgemm / opsparse_spgemm_reg
+ *                            (include/opsparse/core_algo/spgemm/spgemm.hpp:12-17,
+ *                             src/opsparse/core_algo/spgemm/spgemm.cu:16-126)
+ *   ops_spgemm_symbolic   <- h_setup + h_symbolic_binning + h_symbolic + the row_ptr scan
+ *                            (src/opsparse/core_algo/spgemm/spgemm_phases.cu:19-121, spgemm.cu:49)
+ *   ops_spgemm_numeric    <- h_numeric_binning + h_numeric_full_occu
+ *                            (spgemm_phases.cu:123-206)
+ *   ops_flop              <- k_compute_flop (src/opsparse/numeric/compute_flop.cu:9-31)
+ *   status codes 0..5     <- SpgemmStatus (include/opsparse/profile/perf.hpp:16-23)
+ *   ops_timings           <- SpgemmTimings fields (include/opsparse/profile/spgemm_timings.hpp:6-30)
+ *   ops_handle_*          <- SpgemmMeta (include/opsparse/core_algo/spgemm/meta.hpp:15-60),
+ *                            but persistent: streams, pool and workspace survive across calls.
+ */
+#ifndef OPSPARSE_GB300_H_
+#define OPSPARSE_GB300_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct ops_handle_s *ops_handle_t;
+
+/* Status codes.  0..5 have the numeric values of OpSparse's SpgemmStatus. */
+enum ops_status {
+    OPS_OK = 0,
+    OPS_NONSQUARE = 1,         /* A.cols != B.rows */
+    OPS_INT32_OVERFLOW = 2,    /* a row's products or nnz(C) exceed INT32_MAX */
+    OPS_OOM = 3,               /* device allocation failed */
+    OPS_CUDA_ERROR = 4,        /* any other CUDA error */
+    OPS_EXCEPTION = 5,         /* unexpected host-side failure */
+    OPS_INVALID_ARGUMENT = 6,  /* null pointer, negative size, unknown dtype, ... */
+    OPS_INVALID_CSR = 7,       /* a column index outside [0, cols) or a malformed row_ptr */
+    OPS_PROBE_LIMIT = 8,       /* an internal hash table overflowed (a library bug if seen) */
+    OPS_TIMEOUT = 9,           /* a bounded device wait gave up */
+    OPS_NOT_SUPPORTED = 10,    /* no plan / request outside what this build supports */
+    OPS_COUNT_MISMATCH = 11    /* numeric found a different nnz than symbolic (library bug) */
+};
+
+/* Value types. */
+enum ops_dtype { OPS_F64 = 0, OPS_F32 = 1 };
+
+/* Per-call phase times in seconds (CUDA events), filled when timing is enabled on the
+ * handle.  Field names follow OpSparse's SpgemmTimings. */
+typedef struct {
+    double setup;             /* workspace preparation */
+    double symbolic_binning;  /* product count + row classification (one kernel) */
+    double symbolic;          /* per-class symbolic kernels */
+    double reduce;            /* always 0: no separate reduction phase */
+    double numeric_binning;   /* always 0: numeric reuses the symbolic classification */
+    double prefix;            /* row_ptr scan */
+    double allocate;          /* C allocation */
+    double numeric;           /* per-class numeric kernels */
+    double cleanup;           /* always 0: workspace is kept on the handle */
+    double total;
+    int64_t flop;             /* intermediate products, sum over rows */
+    int64_t nnz;              /* nnz(C) */
+    int32_t class_rows[8];    /* rows per class: R8, R16, R32, W, T, D, -, - */
+    int64_t launches;         /* library kernels launched by the call */
+    float kernel_ms[2][8];    /* [symbolic, numeric][class] kernel times (timing level 2) */
+} ops_timings;
+
+/* -------------------------------------------------------------------- handle -- */
+int ops_handle_create(ops_handle_t *handle);
+int ops_handle_destroy(ops_handle_t handle);
+/* Event timing: 0 off, 1 per phase, 2 per phase and per class kernel (events recorded on
+ * each class's own stream around its kernel). */
+int ops_handle_set_timing(ops_handle_t handle, int enable);
+int ops_handle_get_timings(ops_handle_t handle, ops_timings *out);
+/* Upper bound in bytes for the dense-row scratch (default 4 GiB). */
+int ops_handle_set_dense_budget(ops_handle_t handle, size_t bytes);
+/* Where ops_spgemm allocates C: 0 (default) = the handle's stream-ordered pool, release
+ * with ops_free; 1 = cudaMalloc, release with cudaFree (what OpSparse's CSR::drelease
+ * expects). */
+int ops_handle_set_output_malloc(ops_handle_t handle, int use_cuda_malloc);
+/* Message for the last failing call on this handle ("" if none). */
+const char *ops_handle_last_error(ops_handle_t handle);
+const char *ops_status_string(int status);
+
+/* ------------------------------------------------------------------- spgemm -- */
+/* C = A * B in one call (drop-in for opsparse_spgemm).  A is rows_a x cols_a, B is
+ * cols_a x cols_b.  On success *c_rpt, *c_col, *c_val hold device arrays allocated by
+ * the library (ops_handle_set_output_malloc says how to release them) and *c_nnz
+ * receives nnz(C).  Returns after the result is complete (the stream is synchronized).
+ * dtype: OPS_F64 or OPS_F32. */
+int ops_spgemm(ops_handle_t handle, int dtype, int32_t rows_a, int32_t cols_a, int32_t cols_b,
+               const int32_t *a_rpt, const int32_t *a_col, const void *a_val, int64_t a_nnz,
+               const int32_t *b_rpt, const int32_t *b_col, const void *b_val, int64_t b_nnz,
+               int32_t **c_rpt, int32_t **c_col, void **c_val, int64_t *c_nnz, void *stream);
+
+/* Symbolic phase: fills the caller's c_rpt (rows_a + 1 int32, device) with C's row
+ * pointers and returns nnz(C) in *c_nnz.  Keeps the row classification on the handle
+ * for a following ops_spgemm_numeric on the same A and B.  Synchronizes the stream. */
+int ops_spgemm_symbolic(ops_handle_t handle, int32_t rows_a, int32_t cols_a, int32_t cols_b,
+                        const int32_t *a_rpt, const int32_t *a_col, int64_t a_nnz,
+                        const int32_t *b_rpt, const int32_t *b_col, int64_t b_nnz,
+                        int32_t *c_rpt, int64_t *c_nnz, void *stream);
+
+/* Numeric phase: fills the caller's c_col / c_val (nnz(C) each) for the pattern from the
+ * last ops_spgemm_symbolic on this handle (same A and B structure; values may differ).
+ * Asynchronous: returns once the kernels are queued on `stream`. */
+int ops_spgemm_numeric(ops_handle_t handle, int dtype, int32_t rows_a, int32_t cols_a, int32_t cols_b,
+                       const int32_t *a_rpt, const int32_t *a_col, const void *a_val,
+                       const int32_t *b_rpt, const int32_t *b_col, const void *b_val,
+                       const int32_t *c_rpt, int32_t *c_col, void *c_val, void *stream);
+
+/* Checks the device-side error flags raised by the last numeric phase (synchronizes the
+ * stream).  Returns OPS_OK, OPS_PROBE_LIMIT or OPS_COUNT_MISMATCH. */
+int ops_spgemm_check(ops_handle_t handle, void *stream);
+
+/* Per-row intermediate-product counts (row_flop, rows_a int64, device; may be NULL) and
+ * their sum (*total, host).  Synchronizes the stream. */
+int ops_flop(int32_t rows_a, int32_t cols_a, const int32_t *a_rpt, const int32_t *a_col, const int32_t *b_rpt,
+             int64_t *row_flop, int64_t *total, void *stream);
+
+/* Releases a device array that ops_spgemm allocated from the handle's pool
+ * (stream-ordered on `stream`). */
+int ops_free(void *dptr, void *stream);
+
+/* Library version string. */
+const char *ops_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* OPSPARSE_GB300_H_ */

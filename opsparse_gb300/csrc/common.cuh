@@ -1,0 +1,234 @@
+// common.cuh — device building blocks shared by every SpGEMM kernel.
+//
+// Everything here is written for sm_103a: 32-wide warps, warp-synchronous shuffles,
+// __match_any_sync for in-chunk de-duplication, shared-memory CAS for hash slots.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace opsg {
+
+constexpr unsigned kFull = 0xffffffffu;
+constexpr int kEmpty = -1;  // empty hash slot / invalid column
+
+// Row classes.  Each row of C is assigned one class by the setup kernel from its
+// intermediate-product count ("flop") and its A-row length; the symbolic and numeric
+// phases both use this classification, so numeric re-walks exactly what symbolic did.
+enum RowClass : int {
+    kClsR8 = 0,   // flop <= 8,  lenA <= 8 : 8 lanes per row, registers only
+    kClsR16 = 1,  // flop <= 16, lenA <= 16: 16 lanes per row
+    kClsR32 = 2,  // flop <= 32, lenA <= 32: one warp per row
+    kClsW = 3,    // flop <= kWarpFlopMax  : one warp per row, shared-memory hash table
+    kClsT = 4,    // flop <= kBlockFlopMax : one CTA per row, shared-memory hash table
+    kClsD = 5,    // larger                : one CTA per row, dense accumulator in HBM
+    kNumClasses = 6
+};
+
+constexpr int kWarpFlopMax = 128;    // W rows: table of nextpow2(2*flop) <= 256 slots per warp
+constexpr int kWarpTableMax = 256;
+constexpr int kBlockFlopMax = 4096;  // T rows: table of nextpow2(2*flop) <= 8192 slots per CTA
+constexpr int kBlockTableMax = 8192;
+
+// Error bits written by kernels into DevInfo::flags (read back by the host).
+enum : int {
+    kErrRowFlopOverflow = 1,  // a row has more than INT_MAX intermediate products
+    kErrProbeLimit = 2,       // a hash probe sequence exceeded its table (cannot happen if sizes are right)
+    kErrCountMismatch = 4,    // numeric found a different nnz than symbolic
+    kErrBadColumn = 8,        // an input column index is outside [0, cols)
+};
+
+// Device-side counters of one SpGEMM call.  Lives in the handle's workspace.
+struct DevInfo {
+    int counts[kNumClasses];      // rows listed in each class
+    int flags;                    // kErr* bits
+    int max_flop;                 // clamped to INT_MAX
+    unsigned long long total_flop;
+    unsigned long long total_nnz;
+};
+
+__device__ __forceinline__ int lane_id() { return threadIdx.x & 31; }
+
+__device__ __forceinline__ unsigned lanemask_lt()
+{
+    unsigned m;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+    return m;
+}
+
+// Fibonacci hashing: the top log2(TS) bits of key * 2^32/phi.
+__device__ __forceinline__ uint32_t hash_slot(int key, int log_ts)
+{
+    return ((uint32_t)key * 2654435761u) >> (32 - log_ts);
+}
+
+__host__ __device__ __forceinline__ int ceil_log2(int x)
+{
+    int l = 0;
+    while ((1 << l) < x) ++l;
+    return l;
+}
+
+// ----------------------------------------------------------------------------------
+// Value accumulation policies.  S is the per-slot accumulator state (8 bytes in both
+// cases).  FP64: one correctly rounded FMA per product, folded in ascending j — the same
+// sequence the oracle evaluates, so results are bit-identical.  FP32: compensated dot
+// product (Ogita, Rump, Oishi 2005, "Dot2"), rounded to float once at the end.
+template <typename T>
+struct Acc;
+
+template <>
+struct Acc<double> {
+    using S = double;
+    __device__ __forceinline__ static S zero() { return 0.0; }
+    __device__ __forceinline__ static S step(S s, double a, double b) { return __fma_rn(a, b, s); }
+    __device__ __forceinline__ static double fin(S s) { return s; }
+};
+
+template <>
+struct Acc<float> {
+    using S = float2;  // x: running sum, y: running compensation
+    __device__ __forceinline__ static S zero() { return make_float2(0.f, 0.f); }
+    __device__ __forceinline__ static S step(S st, float a, float b)
+    {
+        const float h = __fmul_rn(a, b);        // TwoProduct: h + r == a*b
+        const float r = __fmaf_rn(a, b, -h);
+        const float s = __fadd_rn(st.x, h);     // TwoSum: s + q == st.x + h
+        const float z = __fsub_rn(s, st.x);
+        const float q = __fadd_rn(__fsub_rn(st.x, __fsub_rn(s, z)), __fsub_rn(h, z));
+        return make_float2(s, __fadd_rn(st.y, __fadd_rn(q, r)));
+    }
+    __device__ __forceinline__ static float fin(S st) { return __fadd_rn(st.x, st.y); }
+};
+
+template <typename T>
+__device__ __forceinline__ T shfl(T v, int src, int width = 32)
+{
+    return __shfl_sync(kFull, v, src, width);
+}
+
+// Fold the products of one match group into s, in ascending lane order.  Every lane
+// of the warp must call this (it shuffles).  `members` is the group's lane mask for
+// the group leader and 0 for everyone else; a[] and b[] are the lanes' operands.
+template <typename T>
+__device__ __forceinline__ typename Acc<T>::S fold_group(typename Acc<T>::S s, unsigned members, T a, T b)
+{
+    const int lane = lane_id();
+    while (__any_sync(kFull, members != 0u)) {
+        const int src = members ? (__ffs(members) - 1) : lane;
+        const T am = shfl(a, src);
+        const T bm = shfl(b, src);
+        if (members) {
+            s = Acc<T>::step(s, am, bm);
+            members &= members - 1u;
+        }
+    }
+    return s;
+}
+
+// ----------------------------------------------------------------------------------
+// Warp-cooperative enumeration of a row's intermediate products in j-major order.
+//
+// The A entries [a_begin, a_end) are visited in windows of 32 (window starts at
+// a_begin, a_begin + stride, ...).  For each window the lanes load one A entry each,
+// scan the lengths of the selected B rows, and then walk the window's products in
+// chunks of 32: lane p of a chunk handles product c+p, whose owner A entry is found by
+// a 5-step binary search over the scanned lengths.  f(valid, k, a) is called once per
+// chunk with all 32 lanes converged; k indexes B.col/B.val, a is the owner's A value.
+template <bool kNeedVal, typename T, typename F>
+__device__ __forceinline__ void warp_products(int a_begin, int a_end, int stride, const int *__restrict__ acol,
+                                              const T *__restrict__ aval, const int *__restrict__ brpt, F &&f)
+{
+    const int lane = lane_id();
+    for (int wa = a_begin; wa < a_end; wa += stride) {
+        const int q = wa + lane;
+        int b0 = 0, bl = 0;
+        T av = T(0);
+        if (q < a_end) {
+            const int j = __ldg(acol + q);
+            b0 = __ldg(brpt + j);
+            bl = __ldg(brpt + j + 1) - b0;
+            if (kNeedVal) av = __ldg(aval + q);
+        }
+        int incl = bl;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const int t = __shfl_up_sync(kFull, incl, d);
+            if (lane >= d) incl += t;
+        }
+        const unsigned total = (unsigned)__shfl_sync(kFull, incl, 31);
+        for (unsigned c = 0; c < total; c += 32) {
+            const int p = (int)(c + lane);
+            const bool valid = (unsigned)p < total;
+            int lo = 0;
+#pragma unroll
+            for (int step = 16; step >= 1; step >>= 1) {
+                const int v = __shfl_sync(kFull, incl, lo + step - 1);
+                if (v <= p) lo += step;
+            }
+            const int o_incl = __shfl_sync(kFull, incl, lo);
+            const int o_bl = __shfl_sync(kFull, bl, lo);
+            const int o_b0 = __shfl_sync(kFull, b0, lo);
+            const T o_av = kNeedVal ? shfl(av, lo) : T(0);
+            const int k = o_b0 + (p - (o_incl - o_bl));
+            f(valid, k, o_av);
+        }
+    }
+}
+
+// Claim (or find) the slot of `key` in an open-addressing table of ts = 2^log_ts
+// slots.  Linear probing, bounded by the table size; returns -1 (and raises
+// kErrProbeLimit) only if the table is full, which the sizing rules exclude.
+// *is_new is set when this call inserted the key.
+__device__ __forceinline__ int table_claim(int *keys, int key, int log_ts, bool *is_new, int *flags)
+{
+    const uint32_t mask = (1u << log_ts) - 1u;
+    uint32_t h = hash_slot(key, log_ts);
+    for (uint32_t probe = 0; probe <= mask; ++probe) {
+        const int old = atomicCAS(keys + h, kEmpty, key);
+        if (old == kEmpty) {
+            *is_new = true;
+            return (int)h;
+        }
+        if (old == key) {
+            *is_new = false;
+            return (int)h;
+        }
+        h = (h + 1u) & mask;
+    }
+    atomicOr(flags, kErrProbeLimit);
+    *is_new = false;
+    return -1;
+}
+
+// Block-wide inclusive scan of one int per thread (blockDim.x a multiple of 32, at
+// most 1024).  `warp_sums` is shared scratch of 32 ints.  Returns the inclusive
+// prefix; *total receives the block total.  Contains two __syncthreads().
+__device__ __forceinline__ int block_inclusive_scan(int v, int *warp_sums, int *total)
+{
+    const int lane = lane_id();
+    const int warp = threadIdx.x >> 5;
+    const int nwarps = blockDim.x >> 5;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const int t = __shfl_up_sync(kFull, v, d);
+        if (lane >= d) v += t;
+    }
+    if (lane == 31) warp_sums[warp] = v;
+    __syncthreads();
+    if (warp == 0) {
+        int w = lane < nwarps ? warp_sums[lane] : 0;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const int t = __shfl_up_sync(kFull, w, d);
+            if (lane >= d) w += t;
+        }
+        if (lane < nwarps) warp_sums[lane] = w;
+    }
+    __syncthreads();
+    const int before = warp ? warp_sums[warp - 1] : 0;
+    *total = warp_sums[nwarps - 1];
+    return v + before;
+}
+
+}  // namespace opsg

@@ -1,0 +1,708 @@
+// kernels.cuh — the SpGEMM kernels (setup/binning, symbolic and numeric per row class).
+//
+// Correspondence with OpSparse (paths relative to its source tree):
+//   k_setup            <- k_compute_flop (src/opsparse/numeric/compute_flop.cu:9-31) fused with
+//                         k_symbolic_binning/k_symbolic_binning2 (kernels/binning.cuh:11-81):
+//                         one pass computes each row's product count and appends the row to its
+//                         class list, with no host round trip between count and scatter.
+//   k_reg_rows<G>      <- k_symbolic_shared_hash_pwarp / k_numeric_shared_hash_pwarp
+//                         (kernels/symbolic.cuh:9-72, kernels/numeric.cuh:9-107): rows with at
+//                         most G products are handled by G lanes in registers (match_any
+//                         de-duplication, no table, no sort pass).
+//   k_warp_rows        <- k_*_shared_hash_tb for the small bins (symbolic.cuh:74-130,
+//                         numeric.cuh:109-205): one warp per row, table in shared memory.
+//   k_block_rows       <- the same kernels for the large bins and k_*_max_shared_hash_tb
+//                         (symbolic.cuh:132-261, numeric.cuh:207-302): one CTA per row.
+//   k_dense_rows       <- the global-hash fallback (symbolic.cuh:263-325, numeric.cuh:304-393):
+//                         one CTA per row over a dense accumulator and bitmap in HBM, which
+//                         also yields ascending columns without a sort.
+//
+// Numeric values are folded in ascending j for every output entry (see common.cuh), so
+// all classes produce the same bits as the CPU oracle.
+#pragma once
+
+#include <climits>
+
+#include "common.cuh"
+
+namespace opsg {
+
+template <typename T>
+struct SpgemmArgs {
+    const int *__restrict__ arpt;
+    const int *__restrict__ acol;
+    const T *__restrict__ aval;
+    const int *__restrict__ brpt;
+    const int *__restrict__ bcol;
+    const T *__restrict__ bval;
+    int M;             // rows of A and C
+    int K;             // cols of A == rows of B
+    int N;             // cols of B and C
+    const int *__restrict__ row_flop;
+    int *c_rpt;        // symbolic: per-row nnz written at [r]; numeric: row offsets
+    int *c_col;
+    T *c_val;
+    DevInfo *info;
+};
+
+// 64-bit warp sum.
+__device__ __forceinline__ unsigned long long warp_sum_u64(unsigned long long v)
+{
+#pragma unroll
+    for (int d = 16; d >= 1; d >>= 1) v += __shfl_xor_sync(kFull, v, d);
+    return v;
+}
+
+// Sum of one u64 per thread over the block, added to *dst by one thread.  Every thread
+// of the block must call it.
+__device__ __forceinline__ void block_add_u64(unsigned long long v, unsigned long long *dst)
+{
+    __shared__ unsigned long long s_part[32];
+    v = warp_sum_u64(v);
+    const int warp = threadIdx.x >> 5;
+    if (lane_id() == 0) s_part[warp] = v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned long long t = 0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += s_part[w];
+        if (t) atomicAdd(dst, t);
+    }
+    __syncthreads();
+}
+
+// ==================================================================================
+// Setup: per-row product count, validation of A's columns, class assignment, and the
+// scatter of row ids into per-class lists (lists[c * M + i]).  One warp owns 32
+// consecutive rows; rows with more than 8 A entries are summed cooperatively by the
+// warp.  Rows with no products get nnz 0 immediately and join no list.
+// ==================================================================================
+constexpr int kSetupThreads = 512;
+
+__global__ void __launch_bounds__(kSetupThreads) k_setup(const int *__restrict__ arpt, const int *__restrict__ acol,
+                                                        const int *__restrict__ brpt, int M, int K,
+                                                        int *__restrict__ row_flop, int *__restrict__ lists,
+                                                        int *__restrict__ c_rownnz, DevInfo *info)
+{
+    __shared__ int s_cnt[kNumClasses];
+    __shared__ int s_base[kNumClasses];
+    __shared__ unsigned long long s_flop[kSetupThreads / 32];
+    __shared__ int s_flags;
+    const int lane = lane_id();
+    const int warp = threadIdx.x >> 5;
+    if (threadIdx.x < kNumClasses) s_cnt[threadIdx.x] = 0;
+    if (threadIdx.x == 0) s_flags = 0;
+    __syncthreads();
+
+    const int r = blockIdx.x * kSetupThreads + threadIdx.x;
+    const bool in = r < M;
+    int a0 = 0, a1 = 0;
+    if (in) {
+        a0 = arpt[r];
+        a1 = arpt[r + 1];
+    }
+    const int lenA = a1 - a0;
+    long long flop = 0;
+    bool bad = false;
+    if (in && lenA <= 8) {
+        for (int p = a0; p < a1; ++p) {
+            const int j = __ldg(acol + p);
+            if ((unsigned)j < (unsigned)K) flop += __ldg(brpt + j + 1) - __ldg(brpt + j);
+            else bad = true;
+        }
+    }
+    unsigned heavy = __ballot_sync(kFull, in && lenA > 8);
+    while (heavy) {
+        const int t = __ffs(heavy) - 1;
+        heavy &= heavy - 1u;
+        const int h0 = __shfl_sync(kFull, a0, t);
+        const int h1 = __shfl_sync(kFull, a1, t);
+        unsigned long long s = 0;
+        bool hb = false;
+        for (int p = h0 + lane; p < h1; p += 32) {
+            const int j = __ldg(acol + p);
+            if ((unsigned)j < (unsigned)K) s += (unsigned long long)(__ldg(brpt + j + 1) - __ldg(brpt + j));
+            else hb = true;
+        }
+        s = warp_sum_u64(s);
+        hb = __any_sync(kFull, hb);
+        if (lane == t) {
+            flop = (long long)s;
+            bad = hb;
+        }
+    }
+    if (bad) atomicOr(&s_flags, kErrBadColumn);
+    if (flop > INT_MAX) atomicOr(&s_flags, kErrRowFlopOverflow);
+    const int f32 = flop > INT_MAX ? INT_MAX : (int)flop;
+
+    int cls = -1;
+    if (in) {
+        row_flop[r] = f32;
+        if (flop == 0) {
+            c_rownnz[r] = 0;
+        } else if (flop <= 8 && lenA <= 8) {
+            cls = kClsR8;
+        } else if (flop <= 16 && lenA <= 16) {
+            cls = kClsR16;
+        } else if (flop <= 32 && lenA <= 32) {
+            cls = kClsR32;
+        } else if (flop <= kWarpFlopMax) {
+            cls = kClsW;
+        } else if (flop <= kBlockFlopMax) {
+            cls = kClsT;
+        } else {
+            cls = kClsD;
+        }
+    }
+
+    // Per-class positions: warp rank -> block rank -> global base.
+    int my_off = 0;
+#pragma unroll
+    for (int c = 0; c < kNumClasses; ++c) {
+        const unsigned mk = __ballot_sync(kFull, cls == c);
+        if (mk) {
+            const int leader = __ffs(mk) - 1;
+            int base = 0;
+            if (lane == leader) base = atomicAdd(&s_cnt[c], __popc(mk));
+            base = __shfl_sync(kFull, base, leader);
+            if (cls == c) my_off = base + __popc(mk & lanemask_lt());
+        }
+    }
+    unsigned long long wf = warp_sum_u64((unsigned long long)flop);
+    const unsigned wmax = __reduce_max_sync(kFull, (unsigned)f32);
+    if (lane == 0) s_flop[warp] = wf;
+    __syncthreads();
+    if (threadIdx.x < kNumClasses) {
+        const int n = s_cnt[threadIdx.x];
+        s_base[threadIdx.x] = n ? atomicAdd(&info->counts[threadIdx.x], n) : 0;
+    }
+    if (threadIdx.x == 32) {
+        unsigned long long t = 0;
+        for (int w = 0; w < kSetupThreads / 32; ++w) t += s_flop[w];
+        if (t) atomicAdd(&info->total_flop, t);
+        if (s_flags) atomicOr(&info->flags, s_flags);
+    }
+    if (lane == 0 && wmax) atomicMax(&info->max_flop, (int)wmax);
+    __syncthreads();
+    if (cls >= 0) lists[(size_t)cls * M + s_base[cls] + my_off] = r;
+}
+
+// ==================================================================================
+// R classes: G lanes per row (G = 8, 16, 32), all of the row's products in one chunk.
+// Lane q of a group holds product q; duplicates are found with __match_any_sync, the
+// lowest lane of each match group is its leader.  Symbolic: nnz = number of leaders.
+// Numeric: each leader folds its group in lane order (= ascending j), ranks itself
+// among the group's leaders by column, and writes C directly in sorted position.
+// Grid-stride over the class list; every lane of a warp runs the same trip count.
+// ==================================================================================
+template <int G, bool kNum, typename T>
+__global__ void __launch_bounds__(256) k_reg_rows(SpgemmArgs<T> g, const int *__restrict__ list, int count)
+{
+    using AccT = Acc<T>;
+    using S = typename AccT::S;
+    constexpr int kGroups = 32 / G;
+    const int lane = lane_id();
+    const int q = lane & (G - 1);
+    const unsigned gmask = (G == 32) ? kFull : (((1u << G) - 1u) << (lane & ~(G - 1)));
+    const long long warp0 = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
+    unsigned long long nnz_acc = 0;
+
+    for (long long w = warp0; w * kGroups < count; w += nwarps) {
+        const long long gid = w * kGroups + lane / G;
+        const bool active = gid < count;
+        int r = 0, a0 = 0, lenA = 0;
+        if (active) {
+            r = __ldg(list + gid);
+            a0 = __ldg(g.arpt + r);
+            lenA = __ldg(g.arpt + r + 1) - a0;
+        }
+        int b0 = 0, bl = 0;
+        T av = T(0);
+        if (q < lenA) {
+            const int j = __ldg(g.acol + a0 + q);
+            b0 = __ldg(g.brpt + j);
+            bl = __ldg(g.brpt + j + 1) - b0;
+            if (kNum) av = __ldg(g.aval + a0 + q);
+        }
+        int incl = bl;
+#pragma unroll
+        for (int d = 1; d < G; d <<= 1) {
+            const int t = __shfl_up_sync(kFull, incl, d, G);
+            if (q >= d) incl += t;
+        }
+        const int flop = __shfl_sync(kFull, incl, G - 1, G);
+        const bool valid = q < flop;
+        int lo = 0;
+#pragma unroll
+        for (int step = G / 2; step >= 1; step >>= 1) {
+            const int v = __shfl_sync(kFull, incl, lo + step - 1, G);
+            if (v <= q) lo += step;
+        }
+        const int o_incl = __shfl_sync(kFull, incl, lo, G);
+        const int o_bl = __shfl_sync(kFull, bl, lo, G);
+        const int o_b0 = __shfl_sync(kFull, b0, lo, G);
+        const int k = o_b0 + (q - (o_incl - o_bl));
+        const int col = valid ? __ldg(g.bcol + k) : kEmpty;
+        const unsigned m = __match_any_sync(kFull, col) & gmask;
+        const bool leader = valid && (lane == __ffs(m) - 1);
+
+        if constexpr (!kNum) {
+            const unsigned lb = __ballot_sync(kFull, leader) & gmask;
+            if (active && q == 0) {
+                g.c_rpt[r] = __popc(lb);
+                nnz_acc += (unsigned long long)__popc(lb);
+            }
+        } else {
+            const T o_av = shfl(av, lo + (lane & ~(G - 1)));
+            const T bv = valid ? __ldg(g.bval + k) : T(0);
+            S s = fold_group<T>(AccT::zero(), leader ? m : 0u, o_av, bv);
+            int rank = 0;
+#pragma unroll
+            for (int t = 0; t < G; ++t) {
+                const int ct = __shfl_sync(kFull, col, t, G);
+                const int lt = __shfl_sync(kFull, (int)leader, t, G);
+                rank += (lt && ct < col) ? 1 : 0;
+            }
+            if (leader) {
+                const int pos = __ldg(g.c_rpt + r) + rank;
+                g.c_col[pos] = col;
+                g.c_val[pos] = AccT::fin(s);
+            }
+        }
+    }
+    if constexpr (!kNum) block_add_u64(nnz_acc, &g.info->total_nnz);
+}
+
+// ==================================================================================
+// W class: one warp per row, open-addressing table of nextpow2(2*n) <= kWarpTableMax
+// slots in shared memory (n = flop in symbolic, nnz in numeric).  Products are visited
+// in j-major chunks of 32 by warp_products; within a chunk, match groups are folded by
+// their leader, and chunks are separated by __syncwarp, so each slot sees its
+// contributions in ascending j.  Numeric then compacts the table and places each entry
+// at its rank among the row's columns.
+// ==================================================================================
+constexpr int kWarpRowsThreads = 256;
+
+template <bool kNum, typename T>
+__global__ void __launch_bounds__(kWarpRowsThreads) k_warp_rows(SpgemmArgs<T> g, const int *__restrict__ list,
+                                                                int count)
+{
+    using AccT = Acc<T>;
+    using S = typename AccT::S;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int lane = lane_id();
+    const int warp = threadIdx.x >> 5;
+    constexpr int kWarps = kWarpRowsThreads / 32;
+    S *vals = reinterpret_cast<S *>(smem_raw) + warp * kWarpTableMax;
+    int *keys = reinterpret_cast<int *>(smem_raw + (kNum ? sizeof(S) * kWarps * kWarpTableMax : 0)) +
+                warp * kWarpTableMax;
+    const long long warp0 = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
+    unsigned long long nnz_acc = 0;
+
+    for (long long it = warp0; it < count; it += nwarps) {
+        const int r = __ldg(list + it);
+        const int a0 = __ldg(g.arpt + r);
+        const int a1 = __ldg(g.arpt + r + 1);
+        int n_expect = 0, off = 0;
+        if constexpr (kNum) {
+            off = __ldg(g.c_rpt + r);
+            n_expect = __ldg(g.c_rpt + r + 1) - off;
+        } else {
+            n_expect = __ldg(g.row_flop + r);
+        }
+        const int log_ts = max(5, ceil_log2(2 * max(n_expect, 1)));
+        const int ts = 1 << log_ts;
+        for (int i = lane; i < ts; i += 32) {
+            keys[i] = kEmpty;
+            if constexpr (kNum) vals[i] = AccT::zero();
+        }
+        __syncwarp();
+        int cnt = 0;
+        warp_products<kNum, T>(a0, a1, 32, g.acol, g.aval, g.brpt, [&](bool valid, int k, T av) {
+            const int col = valid ? __ldg(g.bcol + k) : kEmpty;
+            const unsigned m = __match_any_sync(kFull, col);
+            const bool leader = valid && (lane == __ffs(m) - 1);
+            int slot = -1;
+            if (leader) {
+                bool is_new = false;
+                slot = table_claim(keys, col, log_ts, &is_new, &g.info->flags);
+                cnt += is_new ? 1 : 0;
+            }
+            if constexpr (kNum) {
+                const T bv = valid ? __ldg(g.bval + k) : T(0);
+                S s = slot >= 0 ? vals[slot] : AccT::zero();
+                s = fold_group<T>(s, slot >= 0 ? m : 0u, av, bv);
+                if (slot >= 0) vals[slot] = s;
+            }
+            __syncwarp();
+        });
+        if constexpr (!kNum) {
+            const int tot = (int)__reduce_add_sync(kFull, (unsigned)cnt);
+            if (lane == 0) {
+                g.c_rpt[r] = tot;
+                nnz_acc += (unsigned long long)tot;
+            }
+        } else {
+            // In-place compaction: block b of 32 slots writes to positions < 32*(b+1).
+            int n = 0;
+            for (int base = 0; base < ts; base += 32) {
+                const int kk = keys[base + lane];
+                const S vv = vals[base + lane];
+                const bool occ = kk != kEmpty;
+                const unsigned bal = __ballot_sync(kFull, occ);
+                __syncwarp();
+                if (occ) {
+                    const int pos = n + __popc(bal & lanemask_lt());
+                    keys[pos] = kk;
+                    vals[pos] = vv;
+                }
+                n += __popc(bal);
+                __syncwarp();
+            }
+            if (n != n_expect && lane == 0) atomicOr(&g.info->flags, kErrCountMismatch);
+            const int nw = min(n, n_expect);
+            for (int e = lane; e < nw; e += 32) {
+                const int ke = keys[e];
+                int rank = 0;
+                for (int t = 0; t < nw; ++t) rank += keys[t] < ke ? 1 : 0;
+                g.c_col[off + rank] = ke;
+                g.c_val[off + rank] = AccT::fin(vals[e]);
+            }
+            __syncwarp();
+        }
+    }
+    if constexpr (!kNum) block_add_u64(nnz_acc, &g.info->total_nnz);
+}
+
+// ==================================================================================
+// CTA-chunk walk of a row's products in j-major order, shared by the T and D numeric
+// kernels.  A windows of NT entries are scanned block-wide; the window's products are
+// processed NT at a time (thread t holds product c+t).  `claim(valid, col, leader,
+// lane_members)` runs in parallel; then the warps apply their match groups one warp at
+// a time (warp 0 first), so contributions from different warps reach a slot in
+// ascending j.  `apply(warp-converged)` is called by the active warp only.
+// Loop trip counts depend only on block-uniform values, so every thread reaches every
+// barrier.
+// ==================================================================================
+template <int NT, typename T>
+struct ChunkSmem {
+    int incl[NT];
+    int b0[NT];
+    T av[NT];
+    int warp_sums[32];
+};
+
+template <int NT, typename T, typename FClaim, typename FApply>
+__device__ __forceinline__ void block_products_ordered(int a0, int a1, const SpgemmArgs<T> &g, ChunkSmem<NT, T> &cs,
+                                                       FClaim &&claim, FApply &&apply)
+{
+    const int tid = threadIdx.x;
+    const int lane = lane_id();
+    const int warp = tid >> 5;
+    constexpr int kWarps = NT / 32;
+    for (int wa = a0; wa < a1; wa += NT) {
+        const int q = wa + tid;
+        int b0 = 0, bl = 0;
+        T av = T(0);
+        if (q < a1) {
+            const int j = __ldg(g.acol + q);
+            b0 = __ldg(g.brpt + j);
+            bl = __ldg(g.brpt + j + 1) - b0;
+            av = __ldg(g.aval + q);
+        }
+        int wtot = 0;
+        const int incl = block_inclusive_scan(bl, cs.warp_sums, &wtot);
+        cs.incl[tid] = incl;
+        cs.b0[tid] = b0;
+        cs.av[tid] = av;
+        __syncthreads();
+        for (unsigned c = 0; c < (unsigned)wtot; c += NT) {
+            const int p = (int)(c + tid);
+            const bool valid = (unsigned)p < (unsigned)wtot;
+            int lo = 0;
+#pragma unroll
+            for (int step = NT / 2; step >= 1; step >>= 1) {
+                if (cs.incl[lo + step - 1] <= p) lo += step;
+            }
+            const int o_excl = lo ? cs.incl[lo - 1] : 0;
+            const int k = cs.b0[lo] + (p - o_excl);
+            const T oav = cs.av[lo];
+            const int col = valid ? __ldg(g.bcol + k) : kEmpty;
+            const T bv = valid ? __ldg(g.bval + k) : T(0);
+            const unsigned m = __match_any_sync(kFull, col);
+            const bool leader = valid && (lane == __ffs(m) - 1);
+            const int slot = claim(valid, col, leader);
+            for (int w = 0; w < kWarps; ++w) {
+                __syncthreads();
+                if (warp == w) apply(slot, slot >= 0 ? m : 0u, oav, bv);
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// ==================================================================================
+// T class: one CTA (256 threads) per row, shared-memory table of nextpow2(2*n) <=
+// kBlockTableMax slots.  Symbolic: warps insert independent windows (order-free) and
+// the counts are summed.  Numeric: ordered CTA-chunk walk, then the whole table is
+// bitonic-sorted by column (empty slots sort last) and the first nnz entries written.
+// ==================================================================================
+constexpr int kBlockRowsThreads = 256;
+
+template <typename T>
+constexpr size_t block_rows_smem(bool num)
+{
+    return num ? (sizeof(typename Acc<T>::S) + sizeof(int)) * kBlockTableMax + sizeof(ChunkSmem<kBlockRowsThreads, T>)
+               : sizeof(int) * kBlockTableMax;
+}
+
+template <bool kNum, typename T>
+__global__ void __launch_bounds__(kBlockRowsThreads) k_block_rows(SpgemmArgs<T> g, const int *__restrict__ list,
+                                                                  int count)
+{
+    using AccT = Acc<T>;
+    using S = typename AccT::S;
+    constexpr int NT = kBlockRowsThreads;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    S *vals = reinterpret_cast<S *>(smem_raw);
+    int *keys = reinterpret_cast<int *>(smem_raw + (kNum ? sizeof(S) * kBlockTableMax : 0));
+    ChunkSmem<NT, T> &cs = *reinterpret_cast<ChunkSmem<NT, T> *>(smem_raw + (sizeof(S) + sizeof(int)) * kBlockTableMax);
+    __shared__ int s_cnt;
+    const int tid = threadIdx.x;
+    const int lane = lane_id();
+    const int warp = tid >> 5;
+    unsigned long long nnz_acc = 0;
+
+    for (int it = blockIdx.x; it < count; it += gridDim.x) {
+        const int r = __ldg(list + it);
+        const int a0 = __ldg(g.arpt + r);
+        const int a1 = __ldg(g.arpt + r + 1);
+        int n_expect = 0, off = 0;
+        if constexpr (kNum) {
+            off = __ldg(g.c_rpt + r);
+            n_expect = __ldg(g.c_rpt + r + 1) - off;
+        } else {
+            n_expect = __ldg(g.row_flop + r);
+        }
+        const int log_ts = max(6, ceil_log2(2 * max(n_expect, 1)));
+        const int ts = 1 << log_ts;
+        for (int i = tid; i < ts; i += NT) {
+            keys[i] = kEmpty;
+            if constexpr (kNum) vals[i] = AccT::zero();
+        }
+        if (tid == 0) s_cnt = 0;
+        __syncthreads();
+        if constexpr (!kNum) {
+            int cnt = 0;
+            warp_products<false, T>(a0 + warp * 32, a1, NT, g.acol, g.aval, g.brpt, [&](bool valid, int k, T) {
+                const int col = valid ? __ldg(g.bcol + k) : kEmpty;
+                const unsigned m = __match_any_sync(kFull, col);
+                if (valid && lane == __ffs(m) - 1) {
+                    bool is_new = false;
+                    table_claim(keys, col, log_ts, &is_new, &g.info->flags);
+                    cnt += is_new ? 1 : 0;
+                }
+            });
+            cnt = (int)__reduce_add_sync(kFull, (unsigned)cnt);
+            if (lane == 0 && cnt) atomicAdd(&s_cnt, cnt);
+            __syncthreads();
+            if (tid == 0) {
+                g.c_rpt[r] = s_cnt;
+                nnz_acc += (unsigned long long)s_cnt;
+            }
+            __syncthreads();
+        } else {
+            block_products_ordered<NT, T>(
+                a0, a1, g, cs,
+                [&](bool valid, int col, bool leader) -> int {
+                    if (!leader) return -1;
+                    bool is_new = false;
+                    return table_claim(keys, col, log_ts, &is_new, &g.info->flags);
+                },
+                [&](int slot, unsigned members, T a, T b) {
+                    S s = slot >= 0 ? vals[slot] : AccT::zero();
+                    s = fold_group<T>(s, members, a, b);
+                    if (slot >= 0) vals[slot] = s;
+                });
+            // Bitonic sort of the whole table by key (empty -> INT_MAX, sorts last).
+            for (int i = tid; i < ts; i += NT)
+                if (keys[i] == kEmpty) keys[i] = INT_MAX;
+            __syncthreads();
+            for (int kk = 2; kk <= ts; kk <<= 1) {
+                for (int jj = kk >> 1; jj > 0; jj >>= 1) {
+                    for (int i = tid; i < ts; i += NT) {
+                        const int ixj = i ^ jj;
+                        if (ixj > i) {
+                            const int ki = keys[i], kx = keys[ixj];
+                            const bool up = (i & kk) == 0;
+                            if ((ki > kx) == up) {
+                                keys[i] = kx;
+                                keys[ixj] = ki;
+                                const S t = vals[i];
+                                vals[i] = vals[ixj];
+                                vals[ixj] = t;
+                            }
+                        }
+                    }
+                    __syncthreads();
+                }
+            }
+            int n = 0;
+            for (int i = tid; i < ts; i += NT) n += keys[i] != INT_MAX ? 1 : 0;
+            n = (int)__reduce_add_sync(kFull, (unsigned)n);
+            if (lane == 0 && n) atomicAdd(&s_cnt, n);
+            __syncthreads();
+            if (tid == 0 && s_cnt != n_expect) atomicOr(&g.info->flags, kErrCountMismatch);
+            const int nw = min(s_cnt, n_expect);
+            for (int i = tid; i < nw; i += NT) {
+                g.c_col[off + i] = keys[i];
+                g.c_val[off + i] = AccT::fin(vals[i]);
+            }
+            __syncthreads();
+        }
+    }
+    if constexpr (!kNum) block_add_u64(nnz_acc, &g.info->total_nnz);
+}
+
+// ==================================================================================
+// D class: one CTA (512 threads) per row, dense accumulator over all N columns plus a
+// bitmap, both private to the CTA and kept all-zero between rows (each row clears what
+// it touched).  Symbolic: atomicOr on the bitmap counts first insertions.  Numeric:
+// ordered CTA-chunk walk into vals[col]; then the bitmap words between the row's
+// smallest and largest column are split into contiguous per-thread pieces, counted,
+// scanned and walked in order, which emits ascending columns with no sort.
+// ==================================================================================
+constexpr int kDenseRowsThreads = 512;
+
+template <typename T>
+struct DenseScratch {
+    typename Acc<T>::S *vals;  // gridDim.x * N
+    unsigned *bits;            // gridDim.x * words
+    int words;                 // ceil(N / 32)
+};
+
+template <bool kNum, typename T>
+__global__ void __launch_bounds__(kDenseRowsThreads) k_dense_rows(SpgemmArgs<T> g, const int *__restrict__ list,
+                                                                  int count, DenseScratch<T> ds)
+{
+    using AccT = Acc<T>;
+    using S = typename AccT::S;
+    constexpr int NT = kDenseRowsThreads;
+    __shared__ ChunkSmem<NT, T> cs;
+    __shared__ int s_red[3][32];
+    const int tid = threadIdx.x;
+    const int lane = lane_id();
+    const int warp = tid >> 5;
+    constexpr int kWarps = NT / 32;
+    S *vals = ds.vals + (size_t)blockIdx.x * (size_t)g.N;
+    unsigned *bits = ds.bits + (size_t)blockIdx.x * (size_t)ds.words;
+    const unsigned N = (unsigned)g.N;
+    unsigned long long nnz_acc = 0;
+
+    for (int it = blockIdx.x; it < count; it += gridDim.x) {
+        const int r = __ldg(list + it);
+        const int a0 = __ldg(g.arpt + r);
+        const int a1 = __ldg(g.arpt + r + 1);
+        int cnt = 0, kmin = INT_MAX, kmax = -1;
+        if constexpr (!kNum) {
+            warp_products<false, T>(a0 + warp * 32, a1, NT, g.acol, g.aval, g.brpt, [&](bool valid, int k, T) {
+                if (valid) {
+                    const int col = __ldg(g.bcol + k);
+                    if ((unsigned)col < N) {
+                        const unsigned bit = 1u << (col & 31);
+                        const unsigned old = atomicOr(bits + (col >> 5), bit);
+                        cnt += (old & bit) ? 0 : 1;
+                        kmin = min(kmin, col);
+                        kmax = max(kmax, col);
+                    } else {
+                        atomicOr(&g.info->flags, kErrBadColumn);
+                    }
+                }
+            });
+        } else {
+            block_products_ordered<NT, T>(
+                a0, a1, g, cs,
+                [&](bool valid, int col, bool leader) -> int {
+                    if (!leader) return -1;
+                    if ((unsigned)col >= N) return -1;
+                    atomicOr(bits + (col >> 5), 1u << (col & 31));
+                    kmin = min(kmin, col);
+                    kmax = max(kmax, col);
+                    return col;
+                },
+                [&](int slot, unsigned members, T a, T b) {
+                    S s = slot >= 0 ? vals[slot] : AccT::zero();
+                    s = fold_group<T>(s, members, a, b);
+                    if (slot >= 0) vals[slot] = s;
+                });
+        }
+        // Block reduction of (cnt, kmin, kmax).
+        cnt = (int)__reduce_add_sync(kFull, (unsigned)cnt);
+        kmin = __reduce_min_sync(kFull, kmin);
+        kmax = __reduce_max_sync(kFull, kmax);
+        if (lane == 0) {
+            s_red[0][warp] = cnt;
+            s_red[1][warp] = kmin;
+            s_red[2][warp] = kmax;
+        }
+        __syncthreads();
+        if (warp == 0) {
+            int c = lane < kWarps ? s_red[0][lane] : 0;
+            int lo = lane < kWarps ? s_red[1][lane] : INT_MAX;
+            int hi = lane < kWarps ? s_red[2][lane] : -1;
+            c = (int)__reduce_add_sync(kFull, (unsigned)c);
+            lo = __reduce_min_sync(kFull, lo);
+            hi = __reduce_max_sync(kFull, hi);
+            if (lane == 0) {
+                s_red[0][0] = c;
+                s_red[1][0] = lo;
+                s_red[2][0] = hi;
+            }
+        }
+        __syncthreads();
+        const int tot = s_red[0][0];
+        const int lo = s_red[1][0], hi = s_red[2][0];
+        const int w0 = hi >= 0 ? (lo >> 5) : 0;
+        const int nwords = hi >= 0 ? (hi >> 5) - w0 + 1 : 0;
+        if constexpr (!kNum) {
+            if (tid == 0) {
+                g.c_rpt[r] = tot;
+                nnz_acc += (unsigned long long)tot;
+            }
+            for (int w = tid; w < nwords; w += NT) bits[w0 + w] = 0u;
+            __syncthreads();
+        } else {
+            const int off = __ldg(g.c_rpt + r);
+            const int n_expect = __ldg(g.c_rpt + r + 1) - off;
+            const int per = (nwords + NT - 1) / NT;
+            const int wb = min(nwords, tid * per);
+            const int we = min(nwords, wb + per);
+            int mine = 0;
+            for (int w = wb; w < we; ++w) mine += __popc(bits[w0 + w]);
+            int total = 0;
+            const int incl = block_inclusive_scan(mine, cs.warp_sums, &total);
+            if (tid == 0 && total != n_expect) atomicOr(&g.info->flags, kErrCountMismatch);
+            int pos = incl - mine;
+            for (int w = wb; w < we; ++w) {
+                unsigned word = bits[w0 + w];
+                if (word) bits[w0 + w] = 0u;
+                while (word) {
+                    const int b = __ffs(word) - 1;
+                    word &= word - 1u;
+                    const int col = ((w0 + w) << 5) + b;
+                    if (pos < n_expect) {
+                        g.c_col[off + pos] = col;
+                        g.c_val[off + pos] = AccT::fin(vals[col]);
+                    }
+                    vals[col] = AccT::zero();
+                    ++pos;
+                }
+            }
+            __syncthreads();
+        }
+    }
+    if constexpr (!kNum) block_add_u64(nnz_acc, &g.info->total_nnz);
+}
+
+}  // namespace opsg

@@ -1,0 +1,700 @@
+// spgemm.cu — handle, pipeline and C ABI of the GB300 SpGEMM library.
+//
+// Pipeline of one C = A*B (compare src/opsparse/core_algo/spgemm/spgemm.cu:16-62 and
+// spgemm_phases.cu:12-206 of OpSparse):
+//   1. k_setup: product count per row + class lists             (one kernel, no host sync
+//      between count and scatter, unlike h_symbolic_binning's D2H/H2D round trip)
+//   2. read back class sizes and max products                   (host sync #1)
+//   3. symbolic kernels, one stream per non-empty class, joined back onto the caller's
+//      stream with events                                       (multi-stream bin dispatch)
+//   4. exclusive scan of row nnz into C.row_ptr (CUB)
+//   5. read back nnz(C)                                         (host sync #2)
+//   6. C allocated from the handle's stream-ordered pool
+//   7. numeric kernels on the same per-class streams, reusing step 1's classes
+// Workspace (class lists, counters, scan scratch, dense-row scratch) lives in a
+// cudaMemPool owned by the handle and is reused across calls; streams and events are
+// created once per handle, never per call.
+#include <cub/cub.cuh>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+
+#include "kernels.cuh"
+#include "opsparse_gb300.h"
+
+using namespace opsg;
+
+struct ops_handle_s {
+    int device = 0;
+    int num_sms = 0;
+    cudaMemPool_t pool = nullptr;
+    cudaStream_t side[kNumClasses] = {};
+    cudaEvent_t ev_fork = nullptr;
+    cudaEvent_t ev_join[kNumClasses] = {};
+    static constexpr int kNumEv = 8;
+    cudaEvent_t ev_t[kNumEv] = {};
+    cudaEvent_t ev_k[2][kNumClasses][2] = {};  // [phase][class][start, end]
+    bool kmeasured[2][kNumClasses] = {};
+    int timing = 0;
+    long long launches = 0;
+    bool out_malloc = false;  // allocate C with cudaMalloc instead of the pool
+    ops_timings last_t{};
+    size_t dense_budget = size_t(4) << 30;
+
+    // workspace (grow-only)
+    unsigned char *ws = nullptr;
+    size_t ws_bytes = 0;
+    int ws_M = -1;
+    int *lists = nullptr;
+    int *row_flop = nullptr;
+    DevInfo *info = nullptr;
+    void *cub_tmp = nullptr;
+    size_t cub_bytes = 0;
+    DevInfo *h_info = nullptr;  // pinned host mirror
+
+    // dense-row scratch, all-zero between kernels
+    unsigned char *dense = nullptr;
+    size_t dense_bytes = 0;
+    int dense_ctas = 0;
+
+    // plan of the last symbolic phase
+    bool plan_valid = false;
+    int plan_M = 0, plan_K = 0, plan_N = 0;
+    const int *plan_arpt = nullptr, *plan_acol = nullptr, *plan_brpt = nullptr, *plan_bcol = nullptr;
+    int counts[kNumClasses] = {};
+    long long plan_flop = 0;
+    long long plan_nnz = 0;
+
+    std::string last_error;
+};
+
+namespace {
+
+const char *kVersion = "opsparse_gb300 0.1 (sm_103a)";
+
+int status_of(cudaError_t e) { return e == cudaErrorMemoryAllocation ? OPS_OOM : OPS_CUDA_ERROR; }
+
+int fail(ops_handle_s *h, int status, const std::string &msg)
+{
+    if (h) h->last_error = msg;
+    return status;
+}
+
+#define OPS_CUDA(h, expr)                                                                                 \
+    do {                                                                                                  \
+        cudaError_t e_ = (expr);                                                                          \
+        if (e_ != cudaSuccess) {                                                                          \
+            (void)cudaGetLastError();                                                                     \
+            return fail((h), status_of(e_), std::string(#expr) + ": " + cudaGetErrorString(e_));          \
+        }                                                                                                 \
+    } while (0)
+
+#define OPS_CHECK(expr)             \
+    do {                            \
+        int s_ = (expr);            \
+        if (s_ != OPS_OK) return s_; \
+    } while (0)
+
+size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+struct Mat {
+    int rows, cols;
+    const int *rpt, *col;
+    const void *val;
+};
+
+template <typename T>
+void set_smem_attrs()
+{
+    cudaFuncSetAttribute(k_warp_rows<true, T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)(sizeof(typename Acc<T>::S) + sizeof(int)) * kWarpTableMax * (kWarpRowsThreads / 32));
+    cudaFuncSetAttribute(k_block_rows<true, T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)block_rows_smem<T>(true));
+}
+
+int ensure_ws(ops_handle_s *h, int M, cudaStream_t st)
+{
+    if (h->ws && h->ws_M >= M) return OPS_OK;
+    size_t cub_bytes = 0;
+    OPS_CUDA(h, cub::DeviceScan::ExclusiveSum(nullptr, cub_bytes, (int *)nullptr, (int *)nullptr, M + 1, st));
+    const size_t lists_b = align_up(sizeof(int) * (size_t)kNumClasses * (size_t)M, 256);
+    const size_t flop_b = align_up(sizeof(int) * (size_t)M, 256);
+    const size_t info_b = align_up(sizeof(DevInfo), 256);
+    const size_t total = lists_b + flop_b + info_b + align_up(cub_bytes, 256);
+    if (h->ws) {
+        OPS_CUDA(h, cudaFreeAsync(h->ws, st));
+        h->ws = nullptr;
+    }
+    void *p = nullptr;
+    OPS_CUDA(h, cudaMallocFromPoolAsync(&p, total, h->pool, st));
+    h->ws = static_cast<unsigned char *>(p);
+    h->ws_bytes = total;
+    h->ws_M = M;
+    h->lists = reinterpret_cast<int *>(h->ws);
+    h->row_flop = reinterpret_cast<int *>(h->ws + lists_b);
+    h->info = reinterpret_cast<DevInfo *>(h->ws + lists_b + flop_b);
+    h->cub_tmp = h->ws + lists_b + flop_b + info_b;
+    h->cub_bytes = cub_bytes;
+    h->plan_valid = false;
+    return OPS_OK;
+}
+
+// Dense-row scratch: per CTA, N accumulator slots (8 bytes) and ceil(N/32) bitmap words.
+int ensure_dense(ops_handle_s *h, int N, int rows, cudaStream_t st)
+{
+    const size_t words = (size_t)(N + 31) / 32;
+    const size_t per_cta = (size_t)N * 8 + words * 4;
+    int ctas = std::min(rows, 2 * h->num_sms);
+    const size_t by_budget = per_cta ? h->dense_budget / per_cta : (size_t)ctas;
+    ctas = (int)std::max<size_t>(1, std::min<size_t>((size_t)ctas, by_budget));
+    const size_t need = align_up(per_cta * (size_t)ctas, 256) + 256;
+    if (need > h->dense_bytes) {
+        if (h->dense) {
+            OPS_CUDA(h, cudaFreeAsync(h->dense, st));
+            h->dense = nullptr;
+            h->dense_bytes = 0;
+        }
+        void *p = nullptr;
+        OPS_CUDA(h, cudaMallocFromPoolAsync(&p, need, h->pool, st));
+        OPS_CUDA(h, cudaMemsetAsync(p, 0, need, st));
+        h->dense = static_cast<unsigned char *>(p);
+        h->dense_bytes = need;
+    }
+    h->dense_ctas = ctas;
+    return OPS_OK;
+}
+
+template <typename T>
+DenseScratch<T> dense_view(ops_handle_s *h, int N)
+{
+    DenseScratch<T> d;
+    d.words = (N + 31) / 32;
+    d.vals = reinterpret_cast<typename Acc<T>::S *>(h->dense);
+    d.bits = reinterpret_cast<unsigned *>(h->dense + align_up((size_t)N * 8 * (size_t)h->dense_ctas, 256));
+    return d;
+}
+
+int grid_for(long long work_items, int per_block, int cap)
+{
+    long long b = (work_items + per_block - 1) / per_block;
+    return (int)std::max<long long>(1, std::min<long long>(b, cap));
+}
+
+// Launch the kernels of every non-empty class, each on its own stream forked from `st`
+// and joined back into it.
+template <bool kNum, typename T>
+int launch_classes(ops_handle_s *h, const SpgemmArgs<T> &g, cudaStream_t st)
+{
+    OPS_CUDA(h, cudaEventRecord(h->ev_fork, st));
+    const int sms = h->num_sms;
+    for (int c = 0; c < kNumClasses; ++c) {
+        const int n = h->counts[c];
+        if (n <= 0) continue;
+        cudaStream_t s = h->side[c];
+        OPS_CUDA(h, cudaStreamWaitEvent(s, h->ev_fork, 0));
+        const int *list = h->lists + (size_t)c * (size_t)h->plan_M;
+        if (h->timing >= 2) OPS_CUDA(h, cudaEventRecord(h->ev_k[kNum][c][0], s));
+        switch (c) {
+            case kClsR8:
+                k_reg_rows<8, kNum, T><<<grid_for((n + 3) / 4, 8, sms * 8), 256, 0, s>>>(g, list, n);
+                break;
+            case kClsR16:
+                k_reg_rows<16, kNum, T><<<grid_for((n + 1) / 2, 8, sms * 8), 256, 0, s>>>(g, list, n);
+                break;
+            case kClsR32:
+                k_reg_rows<32, kNum, T><<<grid_for(n, 8, sms * 8), 256, 0, s>>>(g, list, n);
+                break;
+            case kClsW: {
+                const size_t smem = (kNum ? sizeof(typename Acc<T>::S) + sizeof(int) : sizeof(int)) *
+                                    (size_t)kWarpTableMax * (kWarpRowsThreads / 32);
+                k_warp_rows<kNum, T><<<grid_for(n, kWarpRowsThreads / 32, sms * 8), kWarpRowsThreads, smem, s>>>(
+                    g, list, n);
+                break;
+            }
+            case kClsT: {
+                const size_t smem = block_rows_smem<T>(kNum);
+                k_block_rows<kNum, T><<<std::min(n, sms * 2), kBlockRowsThreads, smem, s>>>(g, list, n);
+                break;
+            }
+            case kClsD: {
+                k_dense_rows<kNum, T><<<std::min(n, h->dense_ctas), kDenseRowsThreads, 0, s>>>(
+                    g, list, n, dense_view<T>(h, g.N));
+                break;
+            }
+        }
+        OPS_CUDA(h, cudaGetLastError());
+        ++h->launches;
+        if (h->timing >= 2) {
+            OPS_CUDA(h, cudaEventRecord(h->ev_k[kNum][c][1], s));
+            h->kmeasured[kNum][c] = true;
+        }
+        OPS_CUDA(h, cudaEventRecord(h->ev_join[c], s));
+        OPS_CUDA(h, cudaStreamWaitEvent(st, h->ev_join[c], 0));
+    }
+    return OPS_OK;
+}
+
+int check_mat_args(ops_handle_s *h, int rows, int cols, const int *rpt, const int *col, long long nnz)
+{
+    if (rows < 0 || cols < 0 || nnz < 0) return fail(h, OPS_INVALID_ARGUMENT, "negative matrix size");
+    if (nnz > INT_MAX) return fail(h, OPS_INT32_OVERFLOW, "input nnz exceeds INT32_MAX");
+    if (!rpt && rows > 0) return fail(h, OPS_INVALID_ARGUMENT, "null row_ptr");
+    if (!col && nnz > 0) return fail(h, OPS_INVALID_ARGUMENT, "null col_idx");
+    return OPS_OK;
+}
+
+float ev_ms(cudaEvent_t a, cudaEvent_t b)
+{
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, a, b) != cudaSuccess) {
+        (void)cudaGetLastError();
+        return 0.f;
+    }
+    return ms;
+}
+
+int run_symbolic(ops_handle_s *h, const Mat &A, const Mat &B, int *c_rpt, long long *c_nnz, cudaStream_t st)
+{
+    const int M = A.rows;
+    OPS_CHECK(ensure_ws(h, std::max(M, 1), st));
+    h->plan_valid = false;
+    h->launches = 0;
+    std::memset(h->kmeasured, 0, sizeof(h->kmeasured));
+    if (h->timing) OPS_CUDA(h, cudaEventRecord(h->ev_t[0], st));
+    OPS_CUDA(h, cudaMemsetAsync(h->info, 0, sizeof(DevInfo), st));
+    OPS_CUDA(h, cudaMemsetAsync(c_rpt + M, 0, sizeof(int), st));
+    if (h->timing) OPS_CUDA(h, cudaEventRecord(h->ev_t[1], st));
+    if (M > 0) {
+        k_setup<<<(M + kSetupThreads - 1) / kSetupThreads, kSetupThreads, 0, st>>>(A.rpt, A.col, B.rpt, M, A.cols,
+                                                                                 h->row_flop, h->lists, c_rpt, h->info);
+        OPS_CUDA(h, cudaGetLastError());
+        ++h->launches;
+    }
+    OPS_CUDA(h, cudaMemcpyAsync(h->h_info, h->info, sizeof(DevInfo), cudaMemcpyDeviceToHost, st));
+    if (h->timing) OPS_CUDA(h, cudaEventRecord(h->ev_t[2], st));
+    OPS_CUDA(h, cudaStreamSynchronize(st));
+    const DevInfo hi = *h->h_info;
+    if (hi.flags & kErrBadColumn) return fail(h, OPS_INVALID_CSR, "A has a column index outside [0, cols)");
+    if (hi.flags & kErrRowFlopOverflow)
+        return fail(h, OPS_INT32_OVERFLOW, "a row of C has more than INT32_MAX intermediate products");
+    std::memcpy(h->counts, hi.counts, sizeof(h->counts));
+    h->plan_M = M;
+    h->plan_K = A.cols;
+    h->plan_N = B.cols;
+    h->plan_flop = (long long)hi.total_flop;
+    if (h->counts[kClsD] > 0) OPS_CHECK(ensure_dense(h, B.cols, h->counts[kClsD], st));
+
+    SpgemmArgs<double> g{};
+    g.arpt = A.rpt;
+    g.acol = A.col;
+    g.brpt = B.rpt;
+    g.bcol = B.col;
+    g.M = M;
+    g.K = A.cols;
+    g.N = B.cols;
+    g.row_flop = h->row_flop;
+    g.c_rpt = c_rpt;
+    g.info = h->info;
+    OPS_CHECK((launch_classes<false, double>(h, g, st)));
+    if (h->timing) OPS_CUDA(h, cudaEventRecord(h->ev_t[3], st));
+    size_t cb = h->cub_bytes;
+    OPS_CUDA(h, cub::DeviceScan::ExclusiveSum(h->cub_tmp, cb, c_rpt, c_rpt, M + 1, st));
+    if (h->timing) OPS_CUDA(h, cudaEventRecord(h->ev_t[4], st));
+    OPS_CUDA(h, cudaMemcpyAsync(h->h_info, h->info, sizeof(DevInfo), cudaMemcpyDeviceToHost, st));
+    OPS_CUDA(h, cudaStreamSynchronize(st));
+    const DevInfo h2 = *h->h_info;
+    if (h2.flags & kErrBadColumn) return fail(h, OPS_INVALID_CSR, "B has a column index outside [0, cols)");
+    if (h2.flags & kErrProbeLimit) return fail(h, OPS_PROBE_LIMIT, "symbolic hash table overflow");
+    if (h2.total_nnz > (unsigned long long)INT_MAX) return fail(h, OPS_INT32_OVERFLOW, "nnz(C) exceeds INT32_MAX");
+    *c_nnz = (long long)h2.total_nnz;
+    h->plan_nnz = (long long)h2.total_nnz;
+    h->plan_arpt = A.rpt;
+    h->plan_acol = A.col;
+    h->plan_brpt = B.rpt;
+    h->plan_bcol = B.col;
+    h->plan_valid = true;
+    return OPS_OK;
+}
+
+template <typename T>
+int run_numeric(ops_handle_s *h, const Mat &A, const Mat &B, const int *c_rpt, int *c_col, T *c_val, cudaStream_t st)
+{
+    if (!h->plan_valid || h->plan_M != A.rows || h->plan_K != A.cols || h->plan_N != B.cols ||
+        h->plan_arpt != A.rpt || h->plan_acol != A.col || h->plan_brpt != B.rpt || h->plan_bcol != B.col)
+        return fail(h, OPS_NOT_SUPPORTED, "numeric phase without a matching symbolic phase on this handle");
+    if (h->counts[kClsD] > 0) OPS_CHECK(ensure_dense(h, B.cols, h->counts[kClsD], st));
+    OPS_CUDA(h, cudaMemsetAsync(&h->info->flags, 0, sizeof(int), st));
+    SpgemmArgs<T> g{};
+    g.arpt = A.rpt;
+    g.acol = A.col;
+    g.aval = static_cast<const T *>(A.val);
+    g.brpt = B.rpt;
+    g.bcol = B.col;
+    g.bval = static_cast<const T *>(B.val);
+    g.M = A.rows;
+    g.K = A.cols;
+    g.N = B.cols;
+    g.row_flop = h->row_flop;
+    g.c_rpt = const_cast<int *>(c_rpt);
+    g.c_col = c_col;
+    g.c_val = c_val;
+    g.info = h->info;
+    return launch_classes<true, T>(h, g, st);
+}
+
+int check_flags(ops_handle_s *h, cudaStream_t st)
+{
+    OPS_CUDA(h, cudaMemcpyAsync(&h->h_info->flags, &h->info->flags, sizeof(int), cudaMemcpyDeviceToHost, st));
+    OPS_CUDA(h, cudaStreamSynchronize(st));
+    const int f = h->h_info->flags;
+    if (f & kErrCountMismatch) return fail(h, OPS_COUNT_MISMATCH, "numeric nnz differs from symbolic nnz");
+    if (f & kErrProbeLimit) return fail(h, OPS_PROBE_LIMIT, "numeric hash table overflow");
+    if (f & kErrBadColumn) return fail(h, OPS_INVALID_CSR, "column index outside [0, cols)");
+    return OPS_OK;
+}
+
+void fill_timings(ops_handle_s *h, bool with_numeric)
+{
+    ops_timings &t = h->last_t;
+    std::memset(&t, 0, sizeof(t));
+    t.flop = h->plan_flop;
+    t.nnz = h->plan_nnz;
+    for (int c = 0; c < kNumClasses; ++c) t.class_rows[c] = h->counts[c];
+    t.launches = h->launches;
+    for (int ph = 0; ph < 2; ++ph)
+        for (int c = 0; c < kNumClasses; ++c)
+            t.kernel_ms[ph][c] = h->kmeasured[ph][c] ? ev_ms(h->ev_k[ph][c][0], h->ev_k[ph][c][1]) : 0.f;
+    if (!h->timing) return;
+    t.setup = ev_ms(h->ev_t[0], h->ev_t[1]) * 1e-3;
+    t.symbolic_binning = ev_ms(h->ev_t[1], h->ev_t[2]) * 1e-3;
+    t.symbolic = ev_ms(h->ev_t[2], h->ev_t[3]) * 1e-3;
+    t.prefix = ev_ms(h->ev_t[3], h->ev_t[4]) * 1e-3;
+    if (with_numeric) {
+        t.allocate = ev_ms(h->ev_t[4], h->ev_t[5]) * 1e-3;
+        t.numeric = ev_ms(h->ev_t[5], h->ev_t[6]) * 1e-3;
+        t.total = ev_ms(h->ev_t[0], h->ev_t[6]) * 1e-3;
+    } else {
+        t.total = ev_ms(h->ev_t[0], h->ev_t[4]) * 1e-3;
+    }
+}
+
+int dtype_size(int dtype) { return dtype == OPS_F64 ? 8 : (dtype == OPS_F32 ? 4 : 0); }
+
+// Output arrays of ops_spgemm: the handle's pool (stream-ordered) or plain cudaMalloc.
+cudaError_t out_alloc(ops_handle_s *h, void **p, size_t bytes, cudaStream_t st)
+{
+    if (h->out_malloc) return cudaMalloc(p, bytes);
+    return cudaMallocFromPoolAsync(p, bytes, h->pool, st);
+}
+
+void out_free(ops_handle_s *h, void *p, cudaStream_t st)
+{
+    if (!p) return;
+    if (h->out_malloc) {
+        cudaStreamSynchronize(st);
+        cudaFree(p);
+    } else {
+        cudaFreeAsync(p, st);
+    }
+}
+
+}  // namespace
+
+// ================================================================== C ABI ==========
+extern "C" {
+
+const char *ops_version(void) { return kVersion; }
+
+const char *ops_status_string(int s)
+{
+    switch (s) {
+        case OPS_OK: return "ok";
+        case OPS_NONSQUARE: return "nonsquare";
+        case OPS_INT32_OVERFLOW: return "int32_overflow";
+        case OPS_OOM: return "oom";
+        case OPS_CUDA_ERROR: return "cuda_error";
+        case OPS_EXCEPTION: return "exception";
+        case OPS_INVALID_ARGUMENT: return "invalid_argument";
+        case OPS_INVALID_CSR: return "invalid_csr";
+        case OPS_PROBE_LIMIT: return "probe_limit";
+        case OPS_TIMEOUT: return "timeout";
+        case OPS_NOT_SUPPORTED: return "not_supported";
+        case OPS_COUNT_MISMATCH: return "count_mismatch";
+    }
+    return "unknown";
+}
+
+int ops_handle_create(ops_handle_t *out)
+{
+    if (!out) return OPS_INVALID_ARGUMENT;
+    *out = nullptr;
+    ops_handle_s *h = new (std::nothrow) ops_handle_s();
+    if (!h) return OPS_EXCEPTION;
+    cudaError_t e = cudaGetDevice(&h->device);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&h->num_sms, cudaDevAttrMultiProcessorCount, h->device);
+    if (e == cudaSuccess) {
+        cudaMemPoolProps props{};
+        props.allocType = cudaMemAllocationTypePinned;
+        props.location.type = cudaMemLocationTypeDevice;
+        props.location.id = h->device;
+        e = cudaMemPoolCreate(&h->pool, &props);
+    }
+    if (e == cudaSuccess) {
+        uint64_t thr = UINT64_MAX;
+        e = cudaMemPoolSetAttribute(h->pool, cudaMemPoolAttrReleaseThreshold, &thr);
+    }
+    for (int c = 0; c < kNumClasses && e == cudaSuccess; ++c) {
+        e = cudaStreamCreateWithFlags(&h->side[c], cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->ev_join[c], cudaEventDisableTiming);
+    }
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming);
+    for (int i = 0; i < ops_handle_s::kNumEv && e == cudaSuccess; ++i) e = cudaEventCreate(&h->ev_t[i]);
+    for (int ph = 0; ph < 2 && e == cudaSuccess; ++ph)
+        for (int c = 0; c < kNumClasses && e == cudaSuccess; ++c)
+            for (int k = 0; k < 2 && e == cudaSuccess; ++k) e = cudaEventCreate(&h->ev_k[ph][c][k]);
+    if (e == cudaSuccess) e = cudaMallocHost(reinterpret_cast<void **>(&h->h_info), sizeof(DevInfo));
+    if (e == cudaSuccess) {
+        set_smem_attrs<double>();
+        set_smem_attrs<float>();
+        e = cudaGetLastError();
+    }
+    if (e != cudaSuccess) {
+        (void)cudaGetLastError();
+        ops_handle_destroy(h);
+        return status_of(e);
+    }
+    *out = h;
+    return OPS_OK;
+}
+
+int ops_handle_destroy(ops_handle_t h)
+{
+    if (!h) return OPS_OK;
+    cudaDeviceSynchronize();
+    if (h->ws) cudaFree(h->ws);
+    if (h->dense) cudaFree(h->dense);
+    for (int c = 0; c < kNumClasses; ++c) {
+        if (h->side[c]) cudaStreamDestroy(h->side[c]);
+        if (h->ev_join[c]) cudaEventDestroy(h->ev_join[c]);
+    }
+    if (h->ev_fork) cudaEventDestroy(h->ev_fork);
+    for (int i = 0; i < ops_handle_s::kNumEv; ++i)
+        if (h->ev_t[i]) cudaEventDestroy(h->ev_t[i]);
+    for (int ph = 0; ph < 2; ++ph)
+        for (int c = 0; c < kNumClasses; ++c)
+            for (int k = 0; k < 2; ++k)
+                if (h->ev_k[ph][c][k]) cudaEventDestroy(h->ev_k[ph][c][k]);
+    if (h->h_info) cudaFreeHost(h->h_info);
+    if (h->pool) cudaMemPoolDestroy(h->pool);
+    (void)cudaGetLastError();
+    delete h;
+    return OPS_OK;
+}
+
+int ops_handle_set_timing(ops_handle_t h, int enable)
+{
+    if (!h) return OPS_INVALID_ARGUMENT;
+    h->timing = enable < 0 ? 0 : (enable > 2 ? 2 : enable);
+    return OPS_OK;
+}
+
+int ops_handle_get_timings(ops_handle_t h, ops_timings *out)
+{
+    if (!h || !out) return OPS_INVALID_ARGUMENT;
+    *out = h->last_t;
+    return OPS_OK;
+}
+
+int ops_handle_set_dense_budget(ops_handle_t h, size_t bytes)
+{
+    if (!h) return OPS_INVALID_ARGUMENT;
+    h->dense_budget = bytes;
+    return OPS_OK;
+}
+
+int ops_handle_set_output_malloc(ops_handle_t h, int use_cuda_malloc)
+{
+    if (!h) return OPS_INVALID_ARGUMENT;
+    h->out_malloc = use_cuda_malloc != 0;
+    return OPS_OK;
+}
+
+const char *ops_handle_last_error(ops_handle_t h) { return h ? h->last_error.c_str() : "null handle"; }
+
+int ops_spgemm_symbolic(ops_handle_t h, int32_t rows_a, int32_t cols_a, int32_t cols_b, const int32_t *a_rpt,
+                        const int32_t *a_col, int64_t a_nnz, const int32_t *b_rpt, const int32_t *b_col, int64_t b_nnz,
+                        int32_t *c_rpt, int64_t *c_nnz, void *stream)
+{
+    if (!h || !c_rpt || !c_nnz) return fail(h, OPS_INVALID_ARGUMENT, "null handle or output");
+    try {
+        h->last_error.clear();
+        OPS_CHECK(check_mat_args(h, rows_a, cols_a, a_rpt, a_col, a_nnz));
+        OPS_CHECK(check_mat_args(h, cols_a, cols_b, b_rpt, b_col, b_nnz));
+        cudaStream_t st = static_cast<cudaStream_t>(stream);
+        const Mat A{rows_a, cols_a, a_rpt, a_col, nullptr};
+        const Mat B{cols_a, cols_b, b_rpt, b_col, nullptr};
+        long long nnz = 0;
+        OPS_CHECK(run_symbolic(h, A, B, c_rpt, &nnz, st));
+        *c_nnz = nnz;
+        fill_timings(h, false);
+        return OPS_OK;
+    } catch (...) {
+        return fail(h, OPS_EXCEPTION, "exception in ops_spgemm_symbolic");
+    }
+}
+
+int ops_spgemm_numeric(ops_handle_t h, int dtype, int32_t rows_a, int32_t cols_a, int32_t cols_b,
+                       const int32_t *a_rpt, const int32_t *a_col, const void *a_val, const int32_t *b_rpt,
+                       const int32_t *b_col, const void *b_val, const int32_t *c_rpt, int32_t *c_col, void *c_val,
+                       void *stream)
+{
+    if (!h) return OPS_INVALID_ARGUMENT;
+    if (dtype_size(dtype) == 0) return fail(h, OPS_INVALID_ARGUMENT, "unknown dtype");
+    try {
+        h->last_error.clear();
+        cudaStream_t st = static_cast<cudaStream_t>(stream);
+        const Mat A{rows_a, cols_a, a_rpt, a_col, a_val};
+        const Mat B{cols_a, cols_b, b_rpt, b_col, b_val};
+        if (h->plan_nnz > 0 && (!c_col || !c_val || !a_val || !b_val))
+            return fail(h, OPS_INVALID_ARGUMENT, "null values or output");
+        if (dtype == OPS_F64)
+            return run_numeric<double>(h, A, B, c_rpt, c_col, static_cast<double *>(c_val), st);
+        return run_numeric<float>(h, A, B, c_rpt, c_col, static_cast<float *>(c_val), st);
+    } catch (...) {
+        return fail(h, OPS_EXCEPTION, "exception in ops_spgemm_numeric");
+    }
+}
+
+int ops_spgemm_check(ops_handle_t h, void *stream)
+{
+    if (!h) return OPS_INVALID_ARGUMENT;
+    return check_flags(h, static_cast<cudaStream_t>(stream));
+}
+
+int ops_spgemm(ops_handle_t h, int dtype, int32_t rows_a, int32_t cols_a, int32_t cols_b, const int32_t *a_rpt,
+               const int32_t *a_col, const void *a_val, int64_t a_nnz, const int32_t *b_rpt, const int32_t *b_col,
+               const void *b_val, int64_t b_nnz, int32_t **c_rpt, int32_t **c_col, void **c_val, int64_t *c_nnz,
+               void *stream)
+{
+    if (!h || !c_rpt || !c_col || !c_val || !c_nnz) return fail(h, OPS_INVALID_ARGUMENT, "null handle or output");
+    const int vs = dtype_size(dtype);
+    if (vs == 0) return fail(h, OPS_INVALID_ARGUMENT, "unknown dtype");
+    *c_rpt = nullptr;
+    *c_col = nullptr;
+    *c_val = nullptr;
+    *c_nnz = 0;
+    try {
+        h->last_error.clear();
+        OPS_CHECK(check_mat_args(h, rows_a, cols_a, a_rpt, a_col, a_nnz));
+        OPS_CHECK(check_mat_args(h, cols_a, cols_b, b_rpt, b_col, b_nnz));
+        if ((a_nnz > 0 && !a_val) || (b_nnz > 0 && !b_val)) return fail(h, OPS_INVALID_ARGUMENT, "null values");
+        cudaStream_t st = static_cast<cudaStream_t>(stream);
+        const Mat A{rows_a, cols_a, a_rpt, a_col, a_val};
+        const Mat B{cols_a, cols_b, b_rpt, b_col, b_val};
+        void *p = nullptr;
+        OPS_CUDA(h, out_alloc(h, &p, sizeof(int) * ((size_t)rows_a + 1), st));
+        int *rpt = static_cast<int *>(p);
+        long long nnz = 0;
+        int s = run_symbolic(h, A, B, rpt, &nnz, st);
+        if (s != OPS_OK) {
+            out_free(h, rpt, st);
+            return s;
+        }
+        void *col = nullptr, *val = nullptr;
+        cudaError_t e = out_alloc(h, &col, sizeof(int) * (size_t)std::max(nnz, 1LL), st);
+        if (e == cudaSuccess) e = out_alloc(h, &val, (size_t)vs * (size_t)std::max(nnz, 1LL), st);
+        if (h->timing && e == cudaSuccess) e = cudaEventRecord(h->ev_t[5], st);
+        if (e != cudaSuccess) {
+            (void)cudaGetLastError();
+            out_free(h, col, st);
+            out_free(h, rpt, st);
+            return fail(h, status_of(e), std::string("allocating C: ") + cudaGetErrorString(e));
+        }
+        s = dtype == OPS_F64 ? run_numeric<double>(h, A, B, rpt, static_cast<int *>(col), static_cast<double *>(val), st)
+                             : run_numeric<float>(h, A, B, rpt, static_cast<int *>(col), static_cast<float *>(val), st);
+        if (s == OPS_OK && h->timing) {
+            e = cudaEventRecord(h->ev_t[6], st);
+            if (e != cudaSuccess) s = fail(h, status_of(e), "event record");
+        }
+        if (s == OPS_OK) s = check_flags(h, st);
+        if (s != OPS_OK) {
+            out_free(h, val, st);
+            out_free(h, col, st);
+            out_free(h, rpt, st);
+            cudaStreamSynchronize(st);
+            return s;
+        }
+        fill_timings(h, true);
+        *c_rpt = rpt;
+        *c_col = static_cast<int *>(col);
+        *c_val = val;
+        *c_nnz = nnz;
+        return OPS_OK;
+    } catch (...) {
+        return fail(h, OPS_EXCEPTION, "exception in ops_spgemm");
+    }
+}
+
+int ops_free(void *dptr, void *stream)
+{
+    if (!dptr) return OPS_OK;
+    cudaError_t e = cudaFreeAsync(dptr, static_cast<cudaStream_t>(stream));
+    if (e != cudaSuccess) {
+        (void)cudaGetLastError();
+        return status_of(e);
+    }
+    return OPS_OK;
+}
+
+}  // extern "C"
+
+// ------------------------------------------------------------------ ops_flop -------
+namespace {
+__global__ void __launch_bounds__(256) k_flop64(const int *__restrict__ arpt, const int *__restrict__ acol,
+                                                const int *__restrict__ brpt, int M, int K, long long *row_flop,
+                                                unsigned long long *total, int *bad)
+{
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    unsigned long long s = 0;
+    if (r < M) {
+        for (int p = arpt[r]; p < arpt[r + 1]; ++p) {
+            const int j = acol[p];
+            if ((unsigned)j < (unsigned)K) s += (unsigned long long)(brpt[j + 1] - brpt[j]);
+            else atomicOr(bad, 1);
+        }
+        if (row_flop) row_flop[r] = (long long)s;
+    }
+    block_add_u64(s, total);
+}
+}  // namespace
+
+extern "C" int ops_flop(int32_t rows_a, int32_t cols_a, const int32_t *a_rpt, const int32_t *a_col,
+                        const int32_t *b_rpt, int64_t *row_flop, int64_t *total, void *stream)
+{
+    if (rows_a < 0 || !total || (rows_a > 0 && (!a_rpt || !b_rpt))) return OPS_INVALID_ARGUMENT;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    void *p = nullptr;
+    cudaError_t e = cudaMallocAsync(&p, 16, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(p, 0, 16, st);
+    unsigned long long *d_total = static_cast<unsigned long long *>(p);
+    int *d_bad = reinterpret_cast<int *>(d_total + 1);
+    if (e == cudaSuccess && rows_a > 0) {
+        k_flop64<<<(rows_a + 255) / 256, 256, 0, st>>>(a_rpt, a_col, b_rpt, rows_a, cols_a,
+                                                      reinterpret_cast<long long *>(row_flop), d_total, d_bad);
+        e = cudaGetLastError();
+    }
+    unsigned long long h_res[2] = {0, 0};
+    if (e == cudaSuccess) e = cudaMemcpyAsync(h_res, p, 16, cudaMemcpyDeviceToHost, st);
+    if (p) cudaFreeAsync(p, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) {
+        (void)cudaGetLastError();
+        return status_of(e);
+    }
+    if (h_res[1] & 1ull) return OPS_INVALID_CSR;
+    *total = (int64_t)h_res[0];
+    return OPS_OK;
+}

@@ -1,0 +1,143 @@
+"""GPU parity tests: the CUDA library through its C ABI against the CPU oracle.
+
+FP64: row_ptr, col_idx and values are bit-identical to the oracle (both fold each
+entry's contributions in ascending j with one FMA each).  FP32: structure bit-identical;
+values bit-identical to the oracle's FP32 (Dot2) evaluation and within 1e-5 relative of
+the FP64 oracle on the same (float) inputs.
+"""
+import numpy as np
+import pytest
+
+import oracle
+import opsparse_gb300 as ops
+from tests.cases import small_cases
+
+pytestmark = pytest.mark.gpu
+
+CASES = small_cases()
+IDS = [c[0] for c in CASES]
+F32_REL_TOL = 1e-5
+F64_REL_TOL = 1e-12
+
+
+@pytest.fixture(scope="module")
+def handle(cuda):
+    h = ops.Handle(timing=True)
+    yield h
+    h.close()
+
+
+def to_dev(cuda, m, ncols, dtype):
+    rpt, col, val = m
+    return ops.csr_to_device(rpt, col, val, len(rpt) - 1, ncols, dtype=dtype)
+
+
+def run_case(cuda, handle, case, dtype, oneshot=False):
+    name, a, b, ncols = case
+    kcols = len(b[0]) - 1
+    A = to_dev(cuda, a, kcols, dtype)
+    B = to_dev(cuda, b, ncols, dtype)
+    C = handle.spgemm_oneshot(A, B) if oneshot else handle.spgemm(A, B)
+    cuda.cuda.synchronize()
+    return C.to_host()
+
+
+@pytest.mark.parametrize("case", CASES, ids=IDS)
+def test_f64_bit_exact(cuda, handle, case):
+    name, a, b, ncols = case
+    rpt, col, val = run_case(cuda, handle, case, cuda.float64)
+    orpt, ocol, oval = oracle.spgemm(*a, *b, ncols)
+    assert np.array_equal(rpt.astype(np.int64), orpt), name
+    assert np.array_equal(col, ocol), name
+    assert np.array_equal(val.view(np.uint64), oval.view(np.uint64)), name
+    t = handle.timings()
+    assert t["nnz"] == len(ocol)
+
+
+@pytest.mark.parametrize("case", CASES, ids=IDS)
+def test_f32(cuda, handle, case):
+    name, a, b, ncols = case
+    a32 = (a[0], a[1], a[2].astype(np.float32))
+    b32 = (b[0], b[1], b[2].astype(np.float32))
+    rpt, col, val = run_case(cuda, handle, (name, a32, b32, ncols), cuda.float32)
+    orpt, ocol, oval32 = oracle.spgemm(*a32, *b32, ncols, dtype=np.float32)
+    assert np.array_equal(rpt.astype(np.int64), orpt) and np.array_equal(col, ocol)
+    assert np.array_equal(val.view(np.uint32), oval32.view(np.uint32))
+    _, _, oval64 = oracle.spgemm(a[0], a[1], a32[2].astype(np.float64), b[0], b[1], b32[2].astype(np.float64), ncols)
+    nz = oval64 != 0
+    rel = np.abs(val[nz].astype(np.float64) - oval64[nz]) / np.abs(oval64[nz])
+    assert (rel.max() if rel.size else 0.0) <= F32_REL_TOL
+    assert np.all(val[~nz] == 0)
+
+
+@pytest.mark.parametrize("case", CASES[:4] + CASES[6:7], ids=IDS[:4] + IDS[6:7])
+def test_oneshot_matches_two_phase(cuda, handle, case):
+    r1 = run_case(cuda, handle, case, cuda.float64, oneshot=True)
+    r2 = run_case(cuda, handle, case, cuda.float64, oneshot=False)
+    for x, y in zip(r1, r2):
+        assert np.array_equal(x, y)
+
+
+def test_class_coverage(cuda, handle):
+    """The case set reaches every row class."""
+    seen = np.zeros(6, dtype=np.int64)
+    for case in CASES:
+        run_case(cuda, handle, case, cuda.float64)
+        seen += np.array(handle.timings()["class_rows"])
+    assert np.all(seen > 0), seen
+
+
+def test_repeat_and_resize(cuda, handle):
+    """Workspace reuse across calls of different sizes gives identical results."""
+    big = CASES[2]
+    small = CASES[0]
+    first = run_case(cuda, handle, big, cuda.float64)
+    run_case(cuda, handle, small, cuda.float64)
+    again = run_case(cuda, handle, big, cuda.float64)
+    for x, y in zip(first, again):
+        assert np.array_equal(x, y)
+
+
+def test_empty_inputs(cuda, handle):
+    z = (np.zeros(1, np.int32), np.zeros(0, np.int32), np.zeros(0))
+    C = handle.spgemm(ops.csr_to_device(*z, 0, 0), ops.csr_to_device(*z, 0, 0))
+    assert C.nnz == 0 and C.rpt.numel() == 1
+    e = (np.zeros(6, np.int32), np.zeros(0, np.int32), np.zeros(0))
+    A = ops.csr_to_device(*e, 5, 7)
+    B = ops.csr_to_device(np.zeros(8, np.int32), np.zeros(0, np.int32), np.zeros(0), 7, 9)
+    C = handle.spgemm(A, B)
+    assert C.nnz == 0 and np.all(C.rpt.cpu().numpy() == 0)
+
+
+def test_invalid_column_is_reported(cuda, handle):
+    rpt = np.array([0, 2, 3], np.int32)
+    col = np.array([0, 5, 1], np.int32)  # 5 >= cols (3)
+    A = ops.csr_to_device(rpt, col, np.ones(3), 2, 3)
+    with pytest.raises(ops.OpsError) as ei:
+        handle.symbolic(A, A)
+    assert ei.value.status == ops.capi.OPS_INVALID_CSR
+
+
+def test_numeric_without_symbolic_is_rejected(cuda):
+    h = ops.Handle()
+    a = CASES[0][1]
+    A = to_dev(cuda, a, 16384, cuda.float64)
+    c_rpt = cuda.zeros(16385, dtype=cuda.int32, device="cuda")
+    with pytest.raises(ops.OpsError) as ei:
+        h.numeric(A, A, c_rpt, 10)
+    assert ei.value.status == ops.capi.OPS_NOT_SUPPORTED
+    h.close()
+
+
+def test_device_flop_count(cuda):
+    for name, a, b, ncols in CASES[:6]:
+        A = to_dev(cuda, a, len(b[0]) - 1, cuda.float64)
+        B = to_dev(cuda, b, ncols, cuda.float64)
+        assert ops.flop(A, B) == oracle.flop(a[0], a[1], b[0])[0]
+
+
+def test_timings_reported(cuda, handle):
+    run_case(cuda, handle, CASES[2], cuda.float64, oneshot=True)
+    t = handle.timings()
+    assert t["total"] > 0 and t["symbolic"] > 0 and t["numeric"] > 0
+    assert t["flop"] == oracle.flop(CASES[2][1][0], CASES[2][1][1], CASES[2][2][0])[0]
