@@ -284,9 +284,9 @@ def run_ours(args, desc, dt, data, n, rank, world, local_rank):
     balg = bytes_alg(n, n, nnz_a, nnz_a, nnz_c, s)
     achieved = balg / (t_ms * 1e-3) / 1e9
     kms = phases["kernel_ms"]
-    names = ["R8", "R16", "R32", "W", "T", "D"]
+    names = ["R8", "R16", "R32", "W", "E1", "E2", "D"]
     per_kernel = {f"{ph}_{names[c]}": round(kms[i][c], 4) for i, ph in enumerate(("symbolic", "numeric"))
-                  for c in range(6) if kms[i][c] > 0}
+                  for c in range(7) if kms[i][c] > 0}
     line = {
         "metric": METRIC, "value": gflops, "unit": "GFLOPS", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": t_ms, "higher_is_better": True, "scaling": "weak",

@@ -6,11 +6,12 @@
 
 namespace opsparse {
 
-inline constexpr int kNumBin = 6;        // row classes: R8, R16, R32, W, T, D
+inline constexpr int kNumBin = 7;           // row classes: R8, R16, R32, W, E1, E2, D
 inline constexpr int kWarpSize = 32;
-inline constexpr int kRegFlopMax = 32;   // rows with <= 32 products: registers only
-inline constexpr int kWarpFlopMax = 128; // one warp per row, shared-memory table
-inline constexpr int kBlockFlopMax = 4096;  // one CTA per row, shared-memory table; above: dense
+inline constexpr int kRegFlopMax = 32;      // rows with <= 32 products: registers only
+inline constexpr int kWarpFlopMax = 128;    // one warp per row, shared-memory hash table
+inline constexpr int kEsc1FlopMax = 1024;   // 128-thread CTA per row, expand/sort/compress
+inline constexpr int kEsc2FlopMax = 14336;  // 512-thread CTA per row; above: dense accumulator
 
 template <typename Int>
 inline constexpr Int div_up(Int a, Int b)

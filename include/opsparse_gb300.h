@@ -67,7 +67,7 @@ typedef struct {
     double total;
     int64_t flop;             /* intermediate products, sum over rows */
     int64_t nnz;              /* nnz(C) */
-    int32_t class_rows[8];    /* rows per class: R8, R16, R32, W, T, D, -, - */
+    int32_t class_rows[8];    /* rows per class: R8, R16, R32, W, E1, E2, D, - */
     int64_t launches;         /* library kernels launched by the call */
     float kernel_ms[2][8];    /* [symbolic, numeric][class] kernel times (timing level 2) */
 } ops_timings;

@@ -55,8 +55,8 @@ class Timings(C.Structure):
 
     def as_dict(self) -> dict:
         d = {k: getattr(self, k) for k, _ in self._fields_ if k not in ("class_rows", "kernel_ms")}
-        d["class_rows"] = list(self.class_rows)[:6]
-        d["kernel_ms"] = [list(self.kernel_ms[0])[:6], list(self.kernel_ms[1])[:6]]
+        d["class_rows"] = list(self.class_rows)[:7]
+        d["kernel_ms"] = [list(self.kernel_ms[0])[:7], list(self.kernel_ms[1])[:7]]
         return d
 
 

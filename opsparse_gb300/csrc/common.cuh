@@ -16,19 +16,22 @@ constexpr int kEmpty = -1;  // empty hash slot / invalid column
 // intermediate-product count ("flop") and its A-row length; the symbolic and numeric
 // phases both use this classification, so numeric re-walks exactly what symbolic did.
 enum RowClass : int {
-    kClsR8 = 0,   // flop <= 8,  lenA <= 8 : 8 lanes per row, registers only
-    kClsR16 = 1,  // flop <= 16, lenA <= 16: 16 lanes per row
-    kClsR32 = 2,  // flop <= 32, lenA <= 32: one warp per row
-    kClsW = 3,    // flop <= kWarpFlopMax  : one warp per row, shared-memory hash table
-    kClsT = 4,    // flop <= kBlockFlopMax : one CTA per row, shared-memory hash table
-    kClsD = 5,    // larger                : one CTA per row, dense accumulator in HBM
-    kNumClasses = 6
+    kClsR8 = 0,   // flop <= 8,  lenA <= 8  : 8 lanes per row, registers only
+    kClsR16 = 1,  // flop <= 16, lenA <= 16 : 16 lanes per row
+    kClsR32 = 2,  // flop <= 32, lenA <= 32 : one warp per row
+    kClsW = 3,    // flop <= 128            : one warp per row, shared-memory hash table
+    kClsE1 = 4,   // flop <= 1024, lenA <= 1024   : 128-thread CTA per row, expand/sort/compress
+    kClsE2 = 5,   // flop <= 14336, lenA <= 4096  : 512-thread CTA per row, expand/sort/compress
+    kClsD = 6,    // larger                 : one CTA per row, dense accumulator in HBM
+    kNumClasses = 7
 };
 
-constexpr int kWarpFlopMax = 128;    // W rows: table of nextpow2(2*flop) <= 256 slots per warp
+constexpr int kWarpFlopMax = 128;  // W rows: table of nextpow2(2*flop) <= 256 slots per warp
 constexpr int kWarpTableMax = 256;
-constexpr int kBlockFlopMax = 4096;  // T rows: table of nextpow2(2*flop) <= 8192 slots per CTA
-constexpr int kBlockTableMax = 8192;
+constexpr int kEsc1FlopMax = 1024;
+constexpr int kEsc1AMax = 1024;
+constexpr int kEsc2FlopMax = 14336;
+constexpr int kEsc2AMax = 4096;
 
 // Error bits written by kernels into DevInfo::flags (read back by the host).
 enum : int {

@@ -1,0 +1,319 @@
+// esc.cuh — expand / sort / compress rows: one CTA per row for rows with 129..14336
+// intermediate products.  Replaces OpSparse's per-bin shared-hash kernels for its middle
+// and large bins (kernels/symbolic.cuh:74-261, kernels/numeric.cuh:109-302).
+//
+// Every thread of the CTA takes part in every step, so a row costs a few load-latency
+// levels instead of one dependent chain per warp:
+//   1. scan the lengths of the B rows selected by A's row into shared memory;
+//   2. expand: product p (thread-strided) finds its A entry by binary search over that
+//      scan and loads its column key;
+//   symbolic: 3. insert the keys into a shared-memory hash table (order-free) and count;
+//   numeric:  3. stable LSD radix sort of (key, product index), 8-bit digits; each warp
+//                owns a contiguous slice and scatters it in order, so products of equal
+//                key stay in ascending product order (= ascending j);
+//             4. the first element of each key run computes the run's output position
+//                (block scan of run heads) and folds the run's products in order with
+//                one FMA each — the oracle's sequence, bit for bit — then writes C.
+// Loops run to block-uniform bounds; all __syncthreads are reached by every thread.
+#pragma once
+
+#include <climits>
+
+#include "kernels.cuh"
+
+namespace opsg {
+
+constexpr int pow2_at_least(int x)
+{
+    int p = 1;
+    while (p < x) p <<= 1;
+    return p;
+}
+
+template <int NT, int PCAP, int ACAP>
+struct EscShape {
+    static constexpr int kThreads = NT;
+    static constexpr int kWarps = NT / 32;
+    static constexpr int kProducts = PCAP;     // products per row, at most
+    static constexpr int kAEntries = ACAP;     // A entries per row, at most
+    static constexpr int kTable = pow2_at_least(2 * PCAP);  // symbolic hash slots
+    static constexpr int kDigits = 256;
+    // numeric: keys x2 (u32), ids x2 (u16), per-warp digit counters, A-entry scan + B starts
+    static constexpr size_t kNumericSmem = (size_t)PCAP * (4 + 4 + 2 + 2) + (size_t)kWarps * kDigits * 4 +
+                                           (size_t)ACAP * 8 + 32 * 4 + 64;
+    static constexpr size_t kSymbolicSmem = (size_t)kTable * 4 + (size_t)ACAP * 8 + 32 * 4 + 64;
+};
+
+using EscSmall = EscShape<128, 1024, 1024>;
+using EscLarge = EscShape<512, 14336, 4096>;
+
+// Smallest t in [0, n) with incl[t] > p (incl non-decreasing, incl[n-1] > p).
+__device__ __forceinline__ int esc_owner(const int *incl, int n, int p)
+{
+    int lo = 0, hi = n;
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (incl[mid] <= p) lo = mid + 1;
+        else hi = mid;
+    }
+    return lo;
+}
+
+// Warp-cooperative expansion of products [c, c+32) of a row (all 32 lanes call it).
+// One binary search finds the owner A entry o0 of product c; each lane then loads the
+// scan value of entry o0+lane and finds its own owner with a 5-step shuffle search.
+// If the product lies beyond those 32 entries (possible only when B rows are empty)
+// the lane falls back to its own binary search.  Sets *k to the product's index into
+// B.col/B.val and *o to its A entry; returns whether the lane has a product.
+__device__ __forceinline__ bool esc_expand_chunk(const int *s_incl, const int *s_b0, int lenA, int flop, int c,
+                                                 int *o, int *k)
+{
+    const int lane = lane_id();
+    const int p = c + lane;
+    const bool valid = p < flop;
+    const int o0 = esc_owner(s_incl, lenA, c);
+    const int t = o0 + lane;
+    const int it = t < lenA ? s_incl[t] : INT_MAX;
+    int lo = 0;
+#pragma unroll
+    for (int step = 16; step >= 1; step >>= 1) {
+        const int v = __shfl_sync(kFull, it, lo + step - 1);
+        if (v <= p) lo += step;
+    }
+    const int it31 = __shfl_sync(kFull, it, 31);
+    int own = o0 + lo;
+    if (valid && it31 <= p) own = esc_owner(s_incl, lenA, p);
+    *o = own;
+    *k = valid ? s_b0[own] + p - (own ? s_incl[own - 1] : 0) : 0;
+    return valid;
+}
+
+// Block-wide scan of the B-row lengths of A's row into s_incl/s_b0; returns the row's
+// product count.  Caller guarantees lenA <= ACAP.
+template <int NT, typename T>
+__device__ __forceinline__ int esc_scan_row(const SpgemmArgs<T> &g, int a0, int lenA, int *s_incl, int *s_b0,
+                                            int *warp_sums)
+{
+    int running = 0;
+    for (int base = 0; base < lenA; base += NT) {
+        const int q = base + (int)threadIdx.x;
+        int b0 = 0, bl = 0;
+        if (q < lenA) {
+            const int j = __ldg(g.acol + a0 + q);
+            b0 = __ldg(g.brpt + j);
+            bl = __ldg(g.brpt + j + 1) - b0;
+        }
+        int wtot = 0;
+        const int incl = block_inclusive_scan(bl, warp_sums, &wtot);
+        if (q < lenA) {
+            s_incl[q] = running + incl;
+            s_b0[q] = b0;
+        }
+        running += wtot;
+        __syncthreads();
+    }
+    return running;
+}
+
+template <typename Shape, bool kNum, typename T>
+__global__ void __launch_bounds__(Shape::kThreads) k_esc_rows(SpgemmArgs<T> g, const int *__restrict__ list,
+                                                              int count)
+{
+    using AccT = Acc<T>;
+    using S = typename AccT::S;
+    constexpr int NT = Shape::kThreads;
+    constexpr int NW = Shape::kWarps;
+    constexpr int PCAP = Shape::kProducts;
+    constexpr int ACAP = Shape::kAEntries;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int tid = threadIdx.x;
+    const int lane = lane_id();
+    const int warp = tid >> 5;
+    __shared__ int s_warp_sums[32];
+    __shared__ int s_count;
+    unsigned long long nnz_acc = 0;
+
+    // shared memory carve-up
+    unsigned char *p = smem_raw;
+    unsigned *key0 = nullptr, *key1 = nullptr;
+    unsigned short *id0 = nullptr, *id1 = nullptr;
+    int *hist = nullptr, *table = nullptr;
+    if constexpr (kNum) {
+        key0 = reinterpret_cast<unsigned *>(p);
+        p += sizeof(unsigned) * PCAP;
+        key1 = reinterpret_cast<unsigned *>(p);
+        p += sizeof(unsigned) * PCAP;
+        hist = reinterpret_cast<int *>(p);
+        p += sizeof(int) * NW * Shape::kDigits;
+    } else {
+        table = reinterpret_cast<int *>(p);
+        p += sizeof(int) * Shape::kTable;
+    }
+    int *s_incl = reinterpret_cast<int *>(p);
+    p += sizeof(int) * ACAP;
+    int *s_b0 = reinterpret_cast<int *>(p);
+    p += sizeof(int) * ACAP;
+    if constexpr (kNum) {
+        id0 = reinterpret_cast<unsigned short *>(p);
+        p += sizeof(unsigned short) * PCAP;
+        id1 = reinterpret_cast<unsigned short *>(p);
+    }
+    const int key_bits = max(1, ceil_log2(max(g.N, 2)));
+    const int passes = (key_bits + 7) / 8;
+
+    for (int it = blockIdx.x; it < count; it += gridDim.x) {
+        const int r = __ldg(list + it);
+        const int a0 = __ldg(g.arpt + r);
+        const int lenA = __ldg(g.arpt + r + 1) - a0;
+        const int flop = esc_scan_row<NT, T>(g, a0, lenA, s_incl, s_b0, s_warp_sums);
+
+        if constexpr (!kNum) {
+            // ---------------------------------------------------------- symbolic --
+            const int log_ts = max(6, ceil_log2(2 * max(flop, 1)));
+            const int ts = 1 << log_ts;
+            for (int i = tid; i < ts; i += NT) table[i] = kEmpty;
+            if (tid == 0) s_count = 0;
+            __syncthreads();
+            int cnt = 0;
+            for (int c = warp * 32; c < flop; c += NT) {
+                int o, k;
+                if (!esc_expand_chunk(s_incl, s_b0, lenA, flop, c, &o, &k)) continue;
+                const int col = __ldg(g.bcol + k);
+                if ((unsigned)col >= (unsigned)g.N) {
+                    atomicOr(&g.info->flags, kErrBadColumn);
+                    continue;
+                }
+                bool is_new = false;
+                table_claim(table, col, log_ts, &is_new, &g.info->flags);
+                cnt += is_new ? 1 : 0;
+            }
+            cnt = (int)__reduce_add_sync(kFull, (unsigned)cnt);
+            if (lane == 0 && cnt) atomicAdd(&s_count, cnt);
+            __syncthreads();
+            if (tid == 0) {
+                g.c_rpt[r] = s_count;
+                nnz_acc += (unsigned long long)s_count;
+            }
+            __syncthreads();
+        } else {
+            // ----------------------------------------------------------- numeric --
+            const int off = __ldg(g.c_rpt + r);
+            const int n_expect = __ldg(g.c_rpt + r + 1) - off;
+            const int n = flop;
+            for (int c = warp * 32; c < n; c += NT) {
+                int o, k;
+                if (esc_expand_chunk(s_incl, s_b0, lenA, n, c, &o, &k)) {
+                    key0[c + lane] = (unsigned)__ldg(g.bcol + k);
+                    id0[c + lane] = (unsigned short)(c + lane);
+                }
+            }
+            __syncthreads();
+            unsigned *kin = key0, *kout = key1;
+            unsigned short *iin = id0, *iout = id1;
+            const int per = (n + NW - 1) / NW;
+            const int rb = min(n, warp * per);
+            const int re = min(n, rb + per);
+            int *wh = hist + warp * Shape::kDigits;
+            for (int pass = 0; pass < passes; ++pass) {
+                const int shift = 8 * pass;
+                for (int d = lane; d < Shape::kDigits; d += 32) wh[d] = 0;
+                __syncwarp();
+                for (int c = rb; c < re; c += 32) {
+                    const int i = c + lane;
+                    const bool valid = i < re;
+                    const int d = valid ? (int)((kin[i] >> shift) & 255u) : 256 + lane;
+                    const unsigned peers = __match_any_sync(kFull, d);
+                    if (valid && lane == __ffs(peers) - 1) wh[d] += __popc(peers);
+                    __syncwarp();
+                }
+                __syncthreads();
+                // exclusive offsets in (digit, warp) order: element i of the scan is
+                // hist[i % NW][i / NW]
+                constexpr int kPer = NW * Shape::kDigits / NT;
+                int v[kPer];
+                int sum = 0;
+#pragma unroll
+                for (int e = 0; e < kPer; ++e) {
+                    const int i = tid * kPer + e;
+                    v[e] = hist[(i % NW) * Shape::kDigits + i / NW];
+                    sum += v[e];
+                }
+                int tot = 0;
+                const int incl = block_inclusive_scan(sum, s_warp_sums, &tot);
+                int run = incl - sum;
+#pragma unroll
+                for (int e = 0; e < kPer; ++e) {
+                    const int i = tid * kPer + e;
+                    hist[(i % NW) * Shape::kDigits + i / NW] = run;
+                    run += v[e];
+                }
+                __syncthreads();
+                // stable scatter of this warp's slice, 32 elements at a time, in order
+                for (int c = rb; c < re; c += 32) {
+                    const int i = c + lane;
+                    const bool valid = i < re;
+                    const unsigned key = valid ? kin[i] : 0u;
+                    const unsigned short id = valid ? iin[i] : (unsigned short)0;
+                    const int d = valid ? (int)((key >> shift) & 255u) : 256 + lane;
+                    const unsigned peers = __match_any_sync(kFull, d);
+                    const int leader = __ffs(peers) - 1;
+                    int base = 0;
+                    if (lane == leader && valid) base = wh[d];
+                    base = __shfl_sync(kFull, base, leader);
+                    const int pos = base + __popc(peers & lanemask_lt());
+                    __syncwarp();
+                    if (lane == leader && valid) wh[d] = base + __popc(peers);
+                    if (valid) {
+                        kout[pos] = key;
+                        iout[pos] = id;
+                    }
+                    __syncwarp();
+                }
+                __syncthreads();
+                unsigned *tk = kin;
+                kin = kout;
+                kout = tk;
+                unsigned short *ti = iin;
+                iin = iout;
+                iout = ti;
+            }
+            // run heads -> output positions (contiguous element ranges per thread)
+            const int E = (n + NT - 1) / NT;
+            const int ib = min(n, tid * E);
+            const int ie = min(n, ib + E);
+            int heads = 0;
+            for (int i = ib; i < ie; ++i) heads += (i == 0 || kin[i] != kin[i - 1]) ? 1 : 0;
+            int total = 0;
+            const int hincl = block_inclusive_scan(heads, s_warp_sums, &total);
+            if (tid == 0 && total != n_expect) atomicOr(&g.info->flags, kErrCountMismatch);
+            // output position of every run head, kept in the free ping-pong key buffer
+            unsigned *hpos = kout;
+            int pos = hincl - heads;
+            for (int i = ib; i < ie; ++i)
+                if (i == 0 || kin[i] != kin[i - 1]) hpos[i] = (unsigned)pos++;
+            __syncthreads();
+            // heads are processed thread-strided, so neighbouring threads work on
+            // neighbouring runs and their loads and C stores coalesce
+            for (int i = tid; i < n; i += NT) {
+                const unsigned key = kin[i];
+                if (i > 0 && kin[i - 1] == key) continue;
+                S s = AccT::zero();
+                for (int t = i; t < n && kin[t] == key; ++t) {
+                    const int q = iin[t];
+                    const int o = esc_owner(s_incl, lenA, q);
+                    const int k = s_b0[o] + q - (o ? s_incl[o - 1] : 0);
+                    s = AccT::step(s, __ldg(g.aval + a0 + o), __ldg(g.bval + k));
+                }
+                const int hp = (int)hpos[i];
+                if (hp < n_expect) {
+                    g.c_col[off + hp] = (int)key;
+                    g.c_val[off + hp] = AccT::fin(s);
+                }
+            }
+            __syncthreads();
+        }
+    }
+    if constexpr (!kNum) block_add_u64(nnz_acc, &g.info->total_nnz);
+}
+
+}  // namespace opsg

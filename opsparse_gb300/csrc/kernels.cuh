@@ -11,8 +11,8 @@
 //                         de-duplication, no table, no sort pass).
 //   k_warp_rows        <- k_*_shared_hash_tb for the small bins (symbolic.cuh:74-130,
 //                         numeric.cuh:109-205): one warp per row, table in shared memory.
-//   k_block_rows       <- the same kernels for the large bins and k_*_max_shared_hash_tb
-//                         (symbolic.cuh:132-261, numeric.cuh:207-302): one CTA per row.
+//   k_esc_rows (esc.cuh) <- the same kernels for the middle/large bins and
+//                         k_*_max_shared_hash_tb (symbolic.cuh:132-261, numeric.cuh:207-302).
 //   k_dense_rows       <- the global-hash fallback (symbolic.cuh:263-325, numeric.cuh:304-393):
 //                         one CTA per row over a dense accumulator and bitmap in HBM, which
 //                         also yields ascending columns without a sort.
@@ -147,8 +147,10 @@ __global__ void __launch_bounds__(kSetupThreads) k_setup(const int *__restrict__
             cls = kClsR32;
         } else if (flop <= kWarpFlopMax) {
             cls = kClsW;
-        } else if (flop <= kBlockFlopMax) {
-            cls = kClsT;
+        } else if (flop <= kEsc1FlopMax && lenA <= kEsc1AMax) {
+            cls = kClsE1;
+        } else if (flop <= kEsc2FlopMax && lenA <= kEsc2AMax) {
+            cls = kClsE2;
         } else {
             cls = kClsD;
         }
@@ -376,8 +378,7 @@ __global__ void __launch_bounds__(kWarpRowsThreads) k_warp_rows(SpgemmArgs<T> g,
 }
 
 // ==================================================================================
-// CTA-chunk walk of a row's products in j-major order, shared by the T and D numeric
-// kernels.  A windows of NT entries are scanned block-wide; the window's products are
+// CTA-chunk walk of a row's products in j-major order, used by the D numeric kernel.  A windows of NT entries are scanned block-wide; the window's products are
 // processed NT at a time (thread t holds product c+t).  `claim(valid, col, leader,
 // lane_members)` runs in parallel; then the warps apply their match groups one warp at
 // a time (warp 0 first), so contributions from different warps reach a slot in
@@ -440,129 +441,6 @@ __device__ __forceinline__ void block_products_ordered(int a0, int a1, const Spg
         }
         __syncthreads();
     }
-}
-
-// ==================================================================================
-// T class: one CTA (256 threads) per row, shared-memory table of nextpow2(2*n) <=
-// kBlockTableMax slots.  Symbolic: warps insert independent windows (order-free) and
-// the counts are summed.  Numeric: ordered CTA-chunk walk, then the whole table is
-// bitonic-sorted by column (empty slots sort last) and the first nnz entries written.
-// ==================================================================================
-constexpr int kBlockRowsThreads = 256;
-
-template <typename T>
-constexpr size_t block_rows_smem(bool num)
-{
-    return num ? (sizeof(typename Acc<T>::S) + sizeof(int)) * kBlockTableMax + sizeof(ChunkSmem<kBlockRowsThreads, T>)
-               : sizeof(int) * kBlockTableMax;
-}
-
-template <bool kNum, typename T>
-__global__ void __launch_bounds__(kBlockRowsThreads) k_block_rows(SpgemmArgs<T> g, const int *__restrict__ list,
-                                                                  int count)
-{
-    using AccT = Acc<T>;
-    using S = typename AccT::S;
-    constexpr int NT = kBlockRowsThreads;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    S *vals = reinterpret_cast<S *>(smem_raw);
-    int *keys = reinterpret_cast<int *>(smem_raw + (kNum ? sizeof(S) * kBlockTableMax : 0));
-    ChunkSmem<NT, T> &cs = *reinterpret_cast<ChunkSmem<NT, T> *>(smem_raw + (sizeof(S) + sizeof(int)) * kBlockTableMax);
-    __shared__ int s_cnt;
-    const int tid = threadIdx.x;
-    const int lane = lane_id();
-    const int warp = tid >> 5;
-    unsigned long long nnz_acc = 0;
-
-    for (int it = blockIdx.x; it < count; it += gridDim.x) {
-        const int r = __ldg(list + it);
-        const int a0 = __ldg(g.arpt + r);
-        const int a1 = __ldg(g.arpt + r + 1);
-        int n_expect = 0, off = 0;
-        if constexpr (kNum) {
-            off = __ldg(g.c_rpt + r);
-            n_expect = __ldg(g.c_rpt + r + 1) - off;
-        } else {
-            n_expect = __ldg(g.row_flop + r);
-        }
-        const int log_ts = max(6, ceil_log2(2 * max(n_expect, 1)));
-        const int ts = 1 << log_ts;
-        for (int i = tid; i < ts; i += NT) {
-            keys[i] = kEmpty;
-            if constexpr (kNum) vals[i] = AccT::zero();
-        }
-        if (tid == 0) s_cnt = 0;
-        __syncthreads();
-        if constexpr (!kNum) {
-            int cnt = 0;
-            warp_products<false, T>(a0 + warp * 32, a1, NT, g.acol, g.aval, g.brpt, [&](bool valid, int k, T) {
-                const int col = valid ? __ldg(g.bcol + k) : kEmpty;
-                const unsigned m = __match_any_sync(kFull, col);
-                if (valid && lane == __ffs(m) - 1) {
-                    bool is_new = false;
-                    table_claim(keys, col, log_ts, &is_new, &g.info->flags);
-                    cnt += is_new ? 1 : 0;
-                }
-            });
-            cnt = (int)__reduce_add_sync(kFull, (unsigned)cnt);
-            if (lane == 0 && cnt) atomicAdd(&s_cnt, cnt);
-            __syncthreads();
-            if (tid == 0) {
-                g.c_rpt[r] = s_cnt;
-                nnz_acc += (unsigned long long)s_cnt;
-            }
-            __syncthreads();
-        } else {
-            block_products_ordered<NT, T>(
-                a0, a1, g, cs,
-                [&](bool valid, int col, bool leader) -> int {
-                    if (!leader) return -1;
-                    bool is_new = false;
-                    return table_claim(keys, col, log_ts, &is_new, &g.info->flags);
-                },
-                [&](int slot, unsigned members, T a, T b) {
-                    S s = slot >= 0 ? vals[slot] : AccT::zero();
-                    s = fold_group<T>(s, members, a, b);
-                    if (slot >= 0) vals[slot] = s;
-                });
-            // Bitonic sort of the whole table by key (empty -> INT_MAX, sorts last).
-            for (int i = tid; i < ts; i += NT)
-                if (keys[i] == kEmpty) keys[i] = INT_MAX;
-            __syncthreads();
-            for (int kk = 2; kk <= ts; kk <<= 1) {
-                for (int jj = kk >> 1; jj > 0; jj >>= 1) {
-                    for (int i = tid; i < ts; i += NT) {
-                        const int ixj = i ^ jj;
-                        if (ixj > i) {
-                            const int ki = keys[i], kx = keys[ixj];
-                            const bool up = (i & kk) == 0;
-                            if ((ki > kx) == up) {
-                                keys[i] = kx;
-                                keys[ixj] = ki;
-                                const S t = vals[i];
-                                vals[i] = vals[ixj];
-                                vals[ixj] = t;
-                            }
-                        }
-                    }
-                    __syncthreads();
-                }
-            }
-            int n = 0;
-            for (int i = tid; i < ts; i += NT) n += keys[i] != INT_MAX ? 1 : 0;
-            n = (int)__reduce_add_sync(kFull, (unsigned)n);
-            if (lane == 0 && n) atomicAdd(&s_cnt, n);
-            __syncthreads();
-            if (tid == 0 && s_cnt != n_expect) atomicOr(&g.info->flags, kErrCountMismatch);
-            const int nw = min(s_cnt, n_expect);
-            for (int i = tid; i < nw; i += NT) {
-                g.c_col[off + i] = keys[i];
-                g.c_val[off + i] = AccT::fin(vals[i]);
-            }
-            __syncthreads();
-        }
-    }
-    if constexpr (!kNum) block_add_u64(nnz_acc, &g.info->total_nnz);
 }
 
 // ==================================================================================

@@ -22,7 +22,7 @@
 #include <new>
 #include <string>
 
-#include "kernels.cuh"
+#include "esc.cuh"
 #include "opsparse_gb300.h"
 
 using namespace opsg;
@@ -111,8 +111,14 @@ void set_smem_attrs()
 {
     cudaFuncSetAttribute(k_warp_rows<true, T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)(sizeof(typename Acc<T>::S) + sizeof(int)) * kWarpTableMax * (kWarpRowsThreads / 32));
-    cudaFuncSetAttribute(k_block_rows<true, T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)block_rows_smem<T>(true));
+    cudaFuncSetAttribute(k_esc_rows<EscSmall, true, T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)EscSmall::kNumericSmem);
+    cudaFuncSetAttribute(k_esc_rows<EscLarge, true, T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)EscLarge::kNumericSmem);
+    cudaFuncSetAttribute(k_esc_rows<EscSmall, false, T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)EscSmall::kSymbolicSmem);
+    cudaFuncSetAttribute(k_esc_rows<EscLarge, false, T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)EscLarge::kSymbolicSmem);
 }
 
 int ensure_ws(ops_handle_s *h, int M, cudaStream_t st)
@@ -214,9 +220,14 @@ int launch_classes(ops_handle_s *h, const SpgemmArgs<T> &g, cudaStream_t st)
                     g, list, n);
                 break;
             }
-            case kClsT: {
-                const size_t smem = block_rows_smem<T>(kNum);
-                k_block_rows<kNum, T><<<std::min(n, sms * 2), kBlockRowsThreads, smem, s>>>(g, list, n);
+            case kClsE1: {
+                const size_t smem = kNum ? EscSmall::kNumericSmem : EscSmall::kSymbolicSmem;
+                k_esc_rows<EscSmall, kNum, T><<<std::min(n, sms * 8), EscSmall::kThreads, smem, s>>>(g, list, n);
+                break;
+            }
+            case kClsE2: {
+                const size_t smem = kNum ? EscLarge::kNumericSmem : EscLarge::kSymbolicSmem;
+                k_esc_rows<EscLarge, kNum, T><<<std::min(n, sms), EscLarge::kThreads, smem, s>>>(g, list, n);
                 break;
             }
             case kClsD: {

@@ -58,3 +58,22 @@ def test_no_device_work_without_gpu(built):
     lib = capi.load()
     h = ctypes.c_void_p()
     assert lib.ops_handle_create(ctypes.byref(h)) == capi.OPS_CUDA_ERROR
+
+
+def test_reference_benchmark_drivers_compile_against_dropin(built, tmp_path):
+    """OpSparse's own benchmark drivers (benchmarks/opsparse_profile.cu, opsparse_reg.cu)
+    compile and link unchanged against include/opsparse/ and libopsparse.so."""
+    import os
+    from pathlib import Path
+
+    src = Path(os.environ.get("OPSPARSE_SRC", "/root/reference")) / "benchmarks"
+    if not (src / "opsparse_reg.cu").exists():
+        pytest.skip("OpSparse sources not present")
+    nvcc = built._nvcc()
+    for name in ("opsparse_profile", "opsparse_reg"):
+        out = tmp_path / name
+        res = subprocess.run([nvcc, "-std=c++17", f"-I{built.INCLUDE}", f"-I{src}", str(src / f"{name}.cu"), "-o",
+                              str(out), f"-L{built.OUT}", "-lopsparse", "-lopsparse_gb300",
+                              f"-Xlinker=-rpath={built.OUT}"], capture_output=True, text=True)
+        assert res.returncode == 0, res.stdout + res.stderr
+        assert out.exists()

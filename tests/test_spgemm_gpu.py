@@ -80,7 +80,7 @@ def test_oneshot_matches_two_phase(cuda, handle, case):
 
 def test_class_coverage(cuda, handle):
     """The case set reaches every row class."""
-    seen = np.zeros(6, dtype=np.int64)
+    seen = np.zeros(7, dtype=np.int64)
     for case in CASES:
         run_case(cuda, handle, case, cuda.float64)
         seen += np.array(handle.timings()["class_rows"])
