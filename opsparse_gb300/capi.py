@@ -76,6 +76,7 @@ _SIGS = {
     "ops_spgemm_numeric": (C.c_int, [P, C.c_int, I32, I32, I32, P, P, P, P, P, P, P, P, P, P]),
     "ops_spgemm_check": (C.c_int, [P, P]),
     "ops_flop": (C.c_int, [I32, I32, P, P, P, P, C.POINTER(I64), P]),
+    "ops_flop_noalloc": (C.c_int, [I32, I32, P, P, P, P, C.POINTER(I64), P]),
     "ops_free": (C.c_int, [P, P]),
 }
 
