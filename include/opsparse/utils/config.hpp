@@ -11,7 +11,7 @@ inline constexpr int kWarpSize = 32;
 inline constexpr int kRegFlopMax = 32;      // rows with <= 32 products: registers only
 inline constexpr int kWarpFlopMax = 128;    // one warp per row, shared-memory hash table
 inline constexpr int kEsc1FlopMax = 1024;   // 128-thread CTA per row, expand/sort/compress
-inline constexpr int kEsc2FlopMax = 14336;  // 512-thread CTA per row; above: dense accumulator
+inline constexpr int kEsc2FlopMax = 13312;  // 512-thread CTA per row; above: dense accumulator
 
 template <typename Int>
 inline constexpr Int div_up(Int a, Int b)

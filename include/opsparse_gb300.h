@@ -120,6 +120,27 @@ int ops_spgemm_numeric(ops_handle_t handle, int dtype, int32_t rows_a, int32_t c
  * stream).  Returns OPS_OK, OPS_PROBE_LIMIT or OPS_COUNT_MISMATCH. */
 int ops_spgemm_check(ops_handle_t handle, void *stream);
 
+/* ------------------------------------------------------------------ backward -- */
+/* Gradients of loss = sum(dC .* C) for C = A * B with A's, B's and C's patterns fixed
+ * (no counterpart in OpSparse).  c_rpt/c_col is C's pattern as produced by the forward
+ * (ascending columns); dc_val holds dC on it.  Fills da_val (A's pattern) and/or db_val
+ * (B's pattern); either may be NULL.  dA_ij = sum_k B_jk dC_ik folded over k in B's row
+ * order; dB_jk = sum_i A_ij dC_ik folded over ascending i; FP64 uses one FMA per term,
+ * FP32 the Dot2 compensated sum.  The first call for a pattern builds a plan on the handle
+ * (A's transpose order and, if it fits the map budget, each product's position in C);
+ * later calls with the same pattern pointers reuse it.  Asynchronous; ops_spgemm_check
+ * reports OPS_COUNT_MISMATCH if C's pattern lacks a product of A and B. */
+int ops_spgemm_backward(ops_handle_t handle, int dtype, int32_t rows_a, int32_t cols_a, int32_t cols_b,
+                        const int32_t *a_rpt, const int32_t *a_col, const void *a_val, int64_t a_nnz,
+                        const int32_t *b_rpt, const int32_t *b_col, const void *b_val, int64_t b_nnz,
+                        const int32_t *c_rpt, const int32_t *c_col, const void *dc_val,
+                        void *da_val, void *db_val, void *stream);
+/* Largest product -> position map (4 bytes per intermediate product) the backward plan may
+ * keep (default 8 GiB).  Above it, positions are searched in C's rows on every call. */
+int ops_handle_set_map_budget(ops_handle_t handle, size_t bytes);
+/* Products and map mode (1 = map kept) of the current backward plan. */
+int ops_backward_plan_info(ops_handle_t handle, int64_t *products, int *with_map);
+
 /* Per-row intermediate-product counts (row_flop, rows_a int64, device; may be NULL) and
  * their sum (*total, host).  Synchronizes the stream. */
 int ops_flop(int32_t rows_a, int32_t cols_a, const int32_t *a_rpt, const int32_t *a_col, const int32_t *b_rpt,

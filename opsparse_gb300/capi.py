@@ -78,6 +78,9 @@ _SIGS = {
     "ops_flop": (C.c_int, [I32, I32, P, P, P, P, C.POINTER(I64), P]),
     "ops_flop_noalloc": (C.c_int, [I32, I32, P, P, P, P, C.POINTER(I64), P]),
     "ops_free": (C.c_int, [P, P]),
+    "ops_spgemm_backward": (C.c_int, [P, C.c_int, I32, I32, I32, P, P, P, I64, P, P, P, I64, P, P, P, P, P, P]),
+    "ops_handle_set_map_budget": (C.c_int, [P, C.c_size_t]),
+    "ops_backward_plan_info": (C.c_int, [P, C.POINTER(I64), C.POINTER(C.c_int)]),
 }
 
 

@@ -21,17 +21,18 @@ enum RowClass : int {
     kClsR32 = 2,  // flop <= 32, lenA <= 32 : one warp per row
     kClsW = 3,    // flop <= 128            : one warp per row, shared-memory hash table
     kClsE1 = 4,   // flop <= 1024, lenA <= 1024   : 128-thread CTA per row, expand/sort/compress
-    kClsE2 = 5,   // flop <= 14336, lenA <= 4096  : 512-thread CTA per row, expand/sort/compress
+    kClsE2 = 5,   // flop <= 13312, lenA <= 2560  : 512-thread CTA per row, expand/sort/compress
     kClsD = 6,    // larger                 : one CTA per row, dense accumulator in HBM
     kNumClasses = 7
 };
 
+constexpr int kSmallFlopMax = 8;   // R8 rows: symbolic inside k_setup, numeric k_small_rows
 constexpr int kWarpFlopMax = 128;  // W rows: table of nextpow2(2*flop) <= 256 slots per warp
 constexpr int kWarpTableMax = 256;
 constexpr int kEsc1FlopMax = 1024;
 constexpr int kEsc1AMax = 1024;
-constexpr int kEsc2FlopMax = 14336;
-constexpr int kEsc2AMax = 4096;
+constexpr int kEsc2FlopMax = 13312;
+constexpr int kEsc2AMax = 2560;
 
 // Error bits written by kernels into DevInfo::flags (read back by the host).
 enum : int {
@@ -48,6 +49,7 @@ struct DevInfo {
     int max_flop;                 // clamped to INT_MAX
     unsigned long long total_flop;
     unsigned long long total_nnz;
+    int next[2][kNumClasses];     // dynamic row cursors of the [symbolic, numeric] kernels
 };
 
 __device__ __forceinline__ int lane_id() { return threadIdx.x & 31; }
@@ -136,8 +138,9 @@ __device__ __forceinline__ typename Acc<T>::S fold_group(typename Acc<T>::S s, u
 // a_begin, a_begin + stride, ...).  For each window the lanes load one A entry each,
 // scan the lengths of the selected B rows, and then walk the window's products in
 // chunks of 32: lane p of a chunk handles product c+p, whose owner A entry is found by
-// a 5-step binary search over the scanned lengths.  f(valid, k, a) is called once per
-// chunk with all 32 lanes converged; k indexes B.col/B.val, a is the owner's A value.
+// a 5-step binary search over the scanned lengths.  f(valid, k, a, p) is called once per
+// chunk with all 32 lanes converged; k indexes B.col/B.val, a is the owner's A value and
+// p the owner's index into A.col/A.val.
 template <bool kNeedVal, typename T, typename F>
 __device__ __forceinline__ void warp_products(int a_begin, int a_end, int stride, const int *__restrict__ acol,
                                               const T *__restrict__ aval, const int *__restrict__ brpt, F &&f)
@@ -174,7 +177,7 @@ __device__ __forceinline__ void warp_products(int a_begin, int a_end, int stride
             const int o_b0 = __shfl_sync(kFull, b0, lo);
             const T o_av = kNeedVal ? shfl(av, lo) : T(0);
             const int k = o_b0 + (p - (o_incl - o_bl));
-            f(valid, k, o_av);
+            f(valid, k, o_av, wa + lo);
         }
     }
 }

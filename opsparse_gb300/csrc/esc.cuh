@@ -1,4 +1,4 @@
-// esc.cuh — expand / sort / compress rows: one CTA per row for rows with 129..14336
+// esc.cuh — expand / sort / compress rows: one CTA per row for rows with 129..13312
 // intermediate products.  Replaces OpSparse's per-bin shared-hash kernels for its middle
 // and large bins (kernels/symbolic.cuh:74-261, kernels/numeric.cuh:109-302).
 //
@@ -38,14 +38,15 @@ struct EscShape {
     static constexpr int kAEntries = ACAP;     // A entries per row, at most
     static constexpr int kTable = pow2_at_least(2 * PCAP);  // symbolic hash slots
     static constexpr int kDigits = 256;
-    // numeric: keys x2 (u32), ids x2 (u16), per-warp digit counters, A-entry scan + B starts
-    static constexpr size_t kNumericSmem = (size_t)PCAP * (4 + 4 + 2 + 2) + (size_t)kWarps * kDigits * 4 +
+    // numeric: keys x2 (u32), ids x2 (u16), owner per product (u16), per-warp digit
+    // counters, A-entry scan + B row starts
+    static constexpr size_t kNumericSmem = (size_t)PCAP * (4 + 4 + 2 + 2 + 2) + (size_t)kWarps * kDigits * 4 +
                                            (size_t)ACAP * 8 + 32 * 4 + 64;
     static constexpr size_t kSymbolicSmem = (size_t)kTable * 4 + (size_t)ACAP * 8 + 32 * 4 + 64;
 };
 
 using EscSmall = EscShape<128, 1024, 1024>;
-using EscLarge = EscShape<512, 14336, 4096>;
+using EscLarge = EscShape<512, 13312, 2560>;
 
 // Smallest t in [0, n) with incl[t] > p (incl non-decreasing, incl[n-1] > p).
 __device__ __forceinline__ int esc_owner(const int *incl, int n, int p)
@@ -59,8 +60,26 @@ __device__ __forceinline__ int esc_owner(const int *incl, int n, int p)
     return lo;
 }
 
+// Smallest t in [0, n) with incl[t] > p, found by the whole warp (p warp-uniform) with a
+// 32-ary search: each round the lanes probe 32 evenly spaced entries and a ballot
+// narrows the range 32-fold, so n <= 1024 takes two shared-memory round trips.
+__device__ __forceinline__ int warp_owner(const int *incl, int n, int p)
+{
+    const int lane = lane_id();
+    int lo = 0, hi = n;
+    for (;;) {
+        const int step = (hi - lo + 31) >> 5;
+        const int q = lo + (lane + 1) * step - 1;
+        const bool le = q < hi && incl[q] <= p;
+        const int nb = __popc(__ballot_sync(kFull, le));
+        if (step <= 1) return lo + nb;
+        lo += nb * step;
+        hi = min(hi, lo + step);
+    }
+}
+
 // Warp-cooperative expansion of products [c, c+32) of a row (all 32 lanes call it).
-// One binary search finds the owner A entry o0 of product c; each lane then loads the
+// A 32-ary warp search finds the owner A entry o0 of product c; each lane then loads the
 // scan value of entry o0+lane and finds its own owner with a 5-step shuffle search.
 // If the product lies beyond those 32 entries (possible only when B rows are empty)
 // the lane falls back to its own binary search.  Sets *k to the product's index into
@@ -71,7 +90,7 @@ __device__ __forceinline__ bool esc_expand_chunk(const int *s_incl, const int *s
     const int lane = lane_id();
     const int p = c + lane;
     const bool valid = p < flop;
-    const int o0 = esc_owner(s_incl, lenA, c);
+    const int o0 = warp_owner(s_incl, lenA, c);
     const int t = o0 + lane;
     const int it = t < lenA ? s_incl[t] : INT_MAX;
     int lo = 0;
@@ -117,7 +136,7 @@ __device__ __forceinline__ int esc_scan_row(const SpgemmArgs<T> &g, int a0, int 
 
 template <typename Shape, bool kNum, typename T>
 __global__ void __launch_bounds__(Shape::kThreads) k_esc_rows(SpgemmArgs<T> g, const int *__restrict__ list,
-                                                              int count)
+                                                              int count, int *cursor)
 {
     using AccT = Acc<T>;
     using S = typename AccT::S;
@@ -136,7 +155,7 @@ __global__ void __launch_bounds__(Shape::kThreads) k_esc_rows(SpgemmArgs<T> g, c
     // shared memory carve-up
     unsigned char *p = smem_raw;
     unsigned *key0 = nullptr, *key1 = nullptr;
-    unsigned short *id0 = nullptr, *id1 = nullptr;
+    unsigned short *id0 = nullptr, *id1 = nullptr, *own = nullptr;
     int *hist = nullptr, *table = nullptr;
     if constexpr (kNum) {
         key0 = reinterpret_cast<unsigned *>(p);
@@ -157,11 +176,21 @@ __global__ void __launch_bounds__(Shape::kThreads) k_esc_rows(SpgemmArgs<T> g, c
         id0 = reinterpret_cast<unsigned short *>(p);
         p += sizeof(unsigned short) * PCAP;
         id1 = reinterpret_cast<unsigned short *>(p);
+        p += sizeof(unsigned short) * PCAP;
+        own = reinterpret_cast<unsigned short *>(p);
     }
     const int key_bits = max(1, ceil_log2(max(g.N, 2)));
     const int passes = (key_bits + 7) / 8;
 
-    for (int it = blockIdx.x; it < count; it += gridDim.x) {
+    __shared__ int s_row;
+    // rows are taken from a shared cursor, so a CTA that drew heavy rows does not hold
+    // up the kernel while others sit idle
+    for (;;) {
+        if (tid == 0) s_row = atomicAdd(cursor, 1);
+        __syncthreads();
+        const int it = s_row;
+        __syncthreads();
+        if (it >= count) break;
         const int r = __ldg(list + it);
         const int a0 = __ldg(g.arpt + r);
         const int lenA = __ldg(g.arpt + r + 1) - a0;
@@ -205,6 +234,7 @@ __global__ void __launch_bounds__(Shape::kThreads) k_esc_rows(SpgemmArgs<T> g, c
                 if (esc_expand_chunk(s_incl, s_b0, lenA, n, c, &o, &k)) {
                     key0[c + lane] = (unsigned)__ldg(g.bcol + k);
                     id0[c + lane] = (unsigned short)(c + lane);
+                    own[c + lane] = (unsigned short)o;
                 }
             }
             __syncthreads();
@@ -300,7 +330,7 @@ __global__ void __launch_bounds__(Shape::kThreads) k_esc_rows(SpgemmArgs<T> g, c
                 S s = AccT::zero();
                 for (int t = i; t < n && kin[t] == key; ++t) {
                     const int q = iin[t];
-                    const int o = esc_owner(s_incl, lenA, q);
+                    const int o = own[q];
                     const int k = s_b0[o] + q - (o ? s_incl[o - 1] : 0);
                     s = AccT::step(s, __ldg(g.aval + a0 + o), __ldg(g.bval + k));
                 }
@@ -314,6 +344,44 @@ __global__ void __launch_bounds__(Shape::kThreads) k_esc_rows(SpgemmArgs<T> g, c
         }
     }
     if constexpr (!kNum) block_add_u64(nnz_acc, &g.info->total_nnz);
+}
+
+// Orders a class list by product count, largest first, so that with dynamic row
+// scheduling the longest rows start first (longest-processing-time order).  One CTA,
+// bitonic sort of (row_flop, row) in shared memory; lists longer than kLptMax stay as
+// they are.
+constexpr int kLptMax = 4096;
+
+static __global__ void __launch_bounds__(1024) k_sort_heavy_first(int *list, const int *count_ptr,
+                                                           const int *__restrict__ row_flop)
+{
+    __shared__ unsigned long long s_e[kLptMax];
+    const int n = *count_ptr;
+    if (n <= 1 || n > kLptMax) return;
+    int m = 1;
+    while (m < n) m <<= 1;
+    for (int i = threadIdx.x; i < m; i += blockDim.x) {
+        // descending flop == ascending (~flop); ties by row id for determinism
+        s_e[i] = i < n ? ((unsigned long long)(0xffffffffu - (unsigned)row_flop[list[i]]) << 32) | (unsigned)list[i]
+                       : ~0ull;
+    }
+    __syncthreads();
+    for (int k = 2; k <= m; k <<= 1) {
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            for (int i = threadIdx.x; i < m; i += blockDim.x) {
+                const int ixj = i ^ j;
+                if (ixj > i) {
+                    const unsigned long long a = s_e[i], b = s_e[ixj];
+                    if ((a > b) == ((i & k) == 0)) {
+                        s_e[i] = b;
+                        s_e[ixj] = a;
+                    }
+                }
+            }
+            __syncthreads();
+        }
+    }
+    for (int i = threadIdx.x; i < n; i += blockDim.x) list[i] = (int)(s_e[i] & 0xffffffffu);
 }
 
 }  // namespace opsg

@@ -1,0 +1,107 @@
+// internal.hpp — the handle and the error helpers shared by the library's translation
+// units (not part of the C ABI).
+#pragma once
+
+#include <string>
+
+#include "common.cuh"
+#include "opsparse_gb300.h"
+
+using opsg::DevInfo;
+using opsg::kNumClasses;
+
+// Per-pattern state of the fixed-pattern backward (built on first use, kept on the handle).
+struct BackwardPlan {
+    bool valid = false;
+    // key: the pattern it was built for
+    int M = 0, K = 0, N = 0;
+    long long nnz_a = 0, nnz_b = 0;
+    const int *a_rpt = nullptr, *a_col = nullptr, *b_rpt = nullptr, *b_col = nullptr;
+    const int *c_rpt = nullptr, *c_col = nullptr;
+    bool with_map = false;      // product -> position map stored (else binary search per product)
+    long long products = 0;
+    unsigned char *mem = nullptr;
+    size_t bytes = 0;
+    long long *pos_base = nullptr;  // [nnz_a] first product index of each A entry
+    int *pmap = nullptr;            // [products] position in C of each product
+    int *at_ptr = nullptr;          // [K+1] columns of A (transpose row pointers)
+    int *at_ent = nullptr;          // [nnz_a] A entries ordered by (column, row)
+    int *arow = nullptr;            // [nnz_a] row of each A entry
+};
+
+struct ops_handle_s {
+    int device = 0;
+    int num_sms = 0;
+    cudaMemPool_t pool = nullptr;
+    cudaStream_t side[kNumClasses] = {};
+    cudaEvent_t ev_fork = nullptr;
+    cudaEvent_t ev_join[kNumClasses] = {};
+    static constexpr int kNumEv = 8;
+    cudaEvent_t ev_t[kNumEv] = {};
+    cudaEvent_t ev_k[2][kNumClasses][2] = {};  // [phase][class][start, end]
+    bool kmeasured[2][kNumClasses] = {};
+    int timing = 0;
+    long long launches = 0;
+    bool out_malloc = false;  // allocate C with cudaMalloc instead of the pool
+    ops_timings last_t{};
+    size_t dense_budget = size_t(4) << 30;
+
+    // workspace (grow-only)
+    unsigned char *ws = nullptr;
+    size_t ws_bytes = 0;
+    int ws_M = -1;
+    int *lists = nullptr;
+    int *row_flop = nullptr;
+    DevInfo *info = nullptr;
+    void *cub_tmp = nullptr;
+    size_t cub_bytes = 0;
+    DevInfo *h_info = nullptr;  // pinned host mirror
+
+    // dense-row scratch, all-zero between kernels
+    unsigned char *dense = nullptr;
+    size_t dense_bytes = 0;
+    int dense_ctas = 0;
+
+    // plan of the last symbolic phase
+    bool plan_valid = false;
+    int plan_M = 0, plan_K = 0, plan_N = 0;
+    const int *plan_arpt = nullptr, *plan_acol = nullptr, *plan_brpt = nullptr, *plan_bcol = nullptr;
+    int counts[kNumClasses] = {};
+    long long plan_flop = 0;
+    long long plan_nnz = 0;
+
+    size_t map_budget = size_t(8) << 30;  // largest product map the backward may keep
+    BackwardPlan bwd;
+
+    std::string last_error;
+};
+
+namespace opsg_internal {
+
+inline int status_of(cudaError_t e) { return e == cudaErrorMemoryAllocation ? OPS_OOM : OPS_CUDA_ERROR; }
+
+inline int fail(ops_handle_s *h, int status, const std::string &msg)
+{
+    if (h) h->last_error = msg;
+    return status;
+}
+
+inline size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+}  // namespace opsg_internal
+
+#define OPS_CUDA(h, expr)                                                                                      \
+    do {                                                                                                       \
+        cudaError_t e_ = (expr);                                                                               \
+        if (e_ != cudaSuccess) {                                                                               \
+            (void)cudaGetLastError();                                                                          \
+            return opsg_internal::fail((h), opsg_internal::status_of(e_),                                      \
+                                       std::string(#expr) + ": " + cudaGetErrorString(e_));                    \
+        }                                                                                                      \
+    } while (0)
+
+#define OPS_CHECK(expr)              \
+    do {                             \
+        int s_ = (expr);             \
+        if (s_ != OPS_OK) return s_; \
+    } while (0)

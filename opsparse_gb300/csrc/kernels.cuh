@@ -78,14 +78,17 @@ __device__ __forceinline__ void block_add_u64(unsigned long long v, unsigned lon
 // ==================================================================================
 constexpr int kSetupThreads = 512;
 
-__global__ void __launch_bounds__(kSetupThreads) k_setup(const int *__restrict__ arpt, const int *__restrict__ acol,
-                                                        const int *__restrict__ brpt, int M, int K,
-                                                        int *__restrict__ row_flop, int *__restrict__ lists,
-                                                        int *__restrict__ c_rownnz, DevInfo *info)
+static __global__ void __launch_bounds__(kSetupThreads) k_setup(const int *__restrict__ arpt, const int *__restrict__ acol,
+                                                        const int *__restrict__ brpt, const int *__restrict__ bcol,
+                                                        int M, int K, int N, int *__restrict__ row_flop,
+                                                        int *__restrict__ lists, int *__restrict__ c_rownnz,
+                                                        DevInfo *info)
 {
+    __shared__ int s_keys[kSmallFlopMax][kSetupThreads];  // R8 rows: the row's column keys
     __shared__ int s_cnt[kNumClasses];
     __shared__ int s_base[kNumClasses];
     __shared__ unsigned long long s_flop[kSetupThreads / 32];
+    __shared__ unsigned s_small[kSetupThreads / 32];
     __shared__ int s_flags;
     const int lane = lane_id();
     const int warp = threadIdx.x >> 5;
@@ -135,12 +138,30 @@ __global__ void __launch_bounds__(kSetupThreads) k_setup(const int *__restrict__
     const int f32 = flop > INT_MAX ? INT_MAX : (int)flop;
 
     int cls = -1;
+    unsigned small_nnz = 0;
     if (in) {
         row_flop[r] = f32;
         if (flop == 0) {
             c_rownnz[r] = 0;
-        } else if (flop <= 8 && lenA <= 8) {
+        } else if (!bad && flop <= kSmallFlopMax && lenA <= kSmallFlopMax) {
+            // R8 row: its symbolic phase happens here — gather the <= 8 column keys and
+            // count the distinct ones.  These rows join no list; the numeric phase walks
+            // them in row order (k_small_rows).
             cls = kClsR8;
+            int n = 0;
+            for (int p = a0; p < a1; ++p) {
+                const int j = __ldg(acol + p);
+                const int q1 = __ldg(brpt + j + 1);
+                for (int q = __ldg(brpt + j); q < q1; ++q) s_keys[n++][threadIdx.x] = __ldg(bcol + q);
+            }
+            for (int m = 0; m < n; ++m) {
+                const int km = s_keys[m][threadIdx.x];
+                bool dup = (unsigned)km >= (unsigned)N;
+                if (dup) atomicOr(&s_flags, kErrBadColumn);
+                for (int t = 0; t < m && !dup; ++t) dup = s_keys[t][threadIdx.x] == km;
+                small_nnz += dup ? 0u : 1u;
+            }
+            c_rownnz[r] = (int)small_nnz;
         } else if (flop <= 16 && lenA <= 16) {
             cls = kClsR16;
         } else if (flop <= 32 && lenA <= 32) {
@@ -171,7 +192,11 @@ __global__ void __launch_bounds__(kSetupThreads) k_setup(const int *__restrict__
     }
     unsigned long long wf = warp_sum_u64((unsigned long long)flop);
     const unsigned wmax = __reduce_max_sync(kFull, (unsigned)f32);
-    if (lane == 0) s_flop[warp] = wf;
+    const unsigned wsmall = __reduce_add_sync(kFull, small_nnz);
+    if (lane == 0) {
+        s_flop[warp] = wf;
+        s_small[warp] = wsmall;
+    }
     __syncthreads();
     if (threadIdx.x < kNumClasses) {
         const int n = s_cnt[threadIdx.x];
@@ -181,11 +206,82 @@ __global__ void __launch_bounds__(kSetupThreads) k_setup(const int *__restrict__
         unsigned long long t = 0;
         for (int w = 0; w < kSetupThreads / 32; ++w) t += s_flop[w];
         if (t) atomicAdd(&info->total_flop, t);
+        unsigned long long sn = 0;
+        for (int w = 0; w < kSetupThreads / 32; ++w) sn += s_small[w];
+        if (sn) atomicAdd(&info->total_nnz, sn);
         if (s_flags) atomicOr(&info->flags, s_flags);
     }
     if (lane == 0 && wmax) atomicMax(&info->max_flop, (int)wmax);
     __syncthreads();
-    if (cls >= 0) lists[(size_t)cls * M + s_base[cls] + my_off] = r;
+    if (cls > kClsR8) lists[(size_t)cls * M + s_base[cls] + my_off] = r;
+}
+
+// ==================================================================================
+// Numeric phase of the R8 rows (<= 8 products, <= 8 A entries), one thread per row in
+// row order: no list, coalesced row metadata.  The thread gathers its products as
+// (key, a, b) into its own column of shared slots, insertion-sorts them by key — stable,
+// so equal keys keep ascending j — then folds each run with one FMA per product and
+// writes C in column order.
+// ==================================================================================
+constexpr int kSmallThreads = 256;
+
+template <typename T>
+__global__ void __launch_bounds__(kSmallThreads) k_small_rows(SpgemmArgs<T> g)
+{
+    using AccT = Acc<T>;
+    __shared__ int s_key[kSmallFlopMax][kSmallThreads];
+    __shared__ T s_a[kSmallFlopMax][kSmallThreads];
+    __shared__ T s_b[kSmallFlopMax][kSmallThreads];
+    const int t = threadIdx.x;
+    for (int r = blockIdx.x * kSmallThreads + t; r < g.M; r += gridDim.x * kSmallThreads) {
+        const int flop = __ldg(g.row_flop + r);
+        const int a0 = __ldg(g.arpt + r);
+        const int a1 = __ldg(g.arpt + r + 1);
+        if (flop == 0 || flop > kSmallFlopMax || a1 - a0 > kSmallFlopMax) continue;
+        int n = 0;
+        for (int p = a0; p < a1; ++p) {
+            const int j = __ldg(g.acol + p);
+            const T a = __ldg(g.aval + p);
+            const int q1 = __ldg(g.brpt + j + 1);
+            for (int q = __ldg(g.brpt + j); q < q1; ++q) {
+                s_key[n][t] = __ldg(g.bcol + q);
+                s_a[n][t] = a;
+                s_b[n][t] = __ldg(g.bval + q);
+                ++n;
+            }
+        }
+        for (int m = 1; m < n; ++m) {
+            const int k = s_key[m][t];
+            const T a = s_a[m][t], b = s_b[m][t];
+            int i = m - 1;
+            while (i >= 0 && s_key[i][t] > k) {
+                s_key[i + 1][t] = s_key[i][t];
+                s_a[i + 1][t] = s_a[i][t];
+                s_b[i + 1][t] = s_b[i][t];
+                --i;
+            }
+            s_key[i + 1][t] = k;
+            s_a[i + 1][t] = a;
+            s_b[i + 1][t] = b;
+        }
+        const int off = __ldg(g.c_rpt + r);
+        const int n_expect = __ldg(g.c_rpt + r + 1) - off;
+        typename AccT::S acc = AccT::zero();
+        int pos = 0;
+        for (int m = 0; m < n; ++m) {
+            const int k = s_key[m][t];
+            acc = AccT::step(acc, s_a[m][t], s_b[m][t]);
+            if (m + 1 == n || s_key[m + 1][t] != k) {
+                if (pos < n_expect) {
+                    g.c_col[off + pos] = k;
+                    g.c_val[off + pos] = AccT::fin(acc);
+                }
+                ++pos;
+                acc = AccT::zero();
+            }
+        }
+        if (pos != n_expect) atomicOr(&g.info->flags, kErrCountMismatch);
+    }
 }
 
 // ==================================================================================
@@ -321,7 +417,7 @@ __global__ void __launch_bounds__(kWarpRowsThreads) k_warp_rows(SpgemmArgs<T> g,
         }
         __syncwarp();
         int cnt = 0;
-        warp_products<kNum, T>(a0, a1, 32, g.acol, g.aval, g.brpt, [&](bool valid, int k, T av) {
+        warp_products<kNum, T>(a0, a1, 32, g.acol, g.aval, g.brpt, [&](bool valid, int k, T av, int) {
             const int col = valid ? __ldg(g.bcol + k) : kEmpty;
             const unsigned m = __match_any_sync(kFull, col);
             const bool leader = valid && (lane == __ffs(m) - 1);
@@ -484,7 +580,7 @@ __global__ void __launch_bounds__(kDenseRowsThreads) k_dense_rows(SpgemmArgs<T> 
         const int a1 = __ldg(g.arpt + r + 1);
         int cnt = 0, kmin = INT_MAX, kmax = -1;
         if constexpr (!kNum) {
-            warp_products<false, T>(a0 + warp * 32, a1, NT, g.acol, g.aval, g.brpt, [&](bool valid, int k, T) {
+            warp_products<false, T>(a0 + warp * 32, a1, NT, g.acol, g.aval, g.brpt, [&](bool valid, int k, T, int) {
                 if (valid) {
                     const int col = __ldg(g.bcol + k);
                     if ((unsigned)col < N) {

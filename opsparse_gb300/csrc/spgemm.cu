@@ -23,82 +23,15 @@
 #include <string>
 
 #include "esc.cuh"
+#include "internal.hpp"
 #include "opsparse_gb300.h"
 
 using namespace opsg;
-
-struct ops_handle_s {
-    int device = 0;
-    int num_sms = 0;
-    cudaMemPool_t pool = nullptr;
-    cudaStream_t side[kNumClasses] = {};
-    cudaEvent_t ev_fork = nullptr;
-    cudaEvent_t ev_join[kNumClasses] = {};
-    static constexpr int kNumEv = 8;
-    cudaEvent_t ev_t[kNumEv] = {};
-    cudaEvent_t ev_k[2][kNumClasses][2] = {};  // [phase][class][start, end]
-    bool kmeasured[2][kNumClasses] = {};
-    int timing = 0;
-    long long launches = 0;
-    bool out_malloc = false;  // allocate C with cudaMalloc instead of the pool
-    ops_timings last_t{};
-    size_t dense_budget = size_t(4) << 30;
-
-    // workspace (grow-only)
-    unsigned char *ws = nullptr;
-    size_t ws_bytes = 0;
-    int ws_M = -1;
-    int *lists = nullptr;
-    int *row_flop = nullptr;
-    DevInfo *info = nullptr;
-    void *cub_tmp = nullptr;
-    size_t cub_bytes = 0;
-    DevInfo *h_info = nullptr;  // pinned host mirror
-
-    // dense-row scratch, all-zero between kernels
-    unsigned char *dense = nullptr;
-    size_t dense_bytes = 0;
-    int dense_ctas = 0;
-
-    // plan of the last symbolic phase
-    bool plan_valid = false;
-    int plan_M = 0, plan_K = 0, plan_N = 0;
-    const int *plan_arpt = nullptr, *plan_acol = nullptr, *plan_brpt = nullptr, *plan_bcol = nullptr;
-    int counts[kNumClasses] = {};
-    long long plan_flop = 0;
-    long long plan_nnz = 0;
-
-    std::string last_error;
-};
+using namespace opsg_internal;
 
 namespace {
 
 const char *kVersion = "opsparse_gb300 0.1 (sm_103a)";
-
-int status_of(cudaError_t e) { return e == cudaErrorMemoryAllocation ? OPS_OOM : OPS_CUDA_ERROR; }
-
-int fail(ops_handle_s *h, int status, const std::string &msg)
-{
-    if (h) h->last_error = msg;
-    return status;
-}
-
-#define OPS_CUDA(h, expr)                                                                                 \
-    do {                                                                                                  \
-        cudaError_t e_ = (expr);                                                                          \
-        if (e_ != cudaSuccess) {                                                                          \
-            (void)cudaGetLastError();                                                                     \
-            return fail((h), status_of(e_), std::string(#expr) + ": " + cudaGetErrorString(e_));          \
-        }                                                                                                 \
-    } while (0)
-
-#define OPS_CHECK(expr)             \
-    do {                            \
-        int s_ = (expr);            \
-        if (s_ != OPS_OK) return s_; \
-    } while (0)
-
-size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
 struct Mat {
     int rows, cols;
@@ -199,13 +132,21 @@ int launch_classes(ops_handle_s *h, const SpgemmArgs<T> &g, cudaStream_t st)
     for (int c = 0; c < kNumClasses; ++c) {
         const int n = h->counts[c];
         if (n <= 0) continue;
+        if (!kNum && c == kClsR8) continue;  // R8 rows are counted inside k_setup
         cudaStream_t s = h->side[c];
         OPS_CUDA(h, cudaStreamWaitEvent(s, h->ev_fork, 0));
         const int *list = h->lists + (size_t)c * (size_t)h->plan_M;
+        if (!kNum && (c == kClsE2 || c == kClsD) && n > 1 && n <= kLptMax) {
+            // longest rows first; the numeric phase reuses the ordered list
+            k_sort_heavy_first<<<1, 1024, 0, s>>>(h->lists + (size_t)c * (size_t)h->plan_M, &h->info->counts[c],
+                                                  h->row_flop);
+            OPS_CUDA(h, cudaGetLastError());
+            ++h->launches;
+        }
         if (h->timing >= 2) OPS_CUDA(h, cudaEventRecord(h->ev_k[kNum][c][0], s));
         switch (c) {
-            case kClsR8:
-                k_reg_rows<8, kNum, T><<<grid_for((n + 3) / 4, 8, sms * 8), 256, 0, s>>>(g, list, n);
+            case kClsR8:  // numeric only: walks the rows in order
+                k_small_rows<T><<<grid_for(g.M, kSmallThreads, sms * 8), kSmallThreads, 0, s>>>(g);
                 break;
             case kClsR16:
                 k_reg_rows<16, kNum, T><<<grid_for((n + 1) / 2, 8, sms * 8), 256, 0, s>>>(g, list, n);
@@ -222,12 +163,14 @@ int launch_classes(ops_handle_s *h, const SpgemmArgs<T> &g, cudaStream_t st)
             }
             case kClsE1: {
                 const size_t smem = kNum ? EscSmall::kNumericSmem : EscSmall::kSymbolicSmem;
-                k_esc_rows<EscSmall, kNum, T><<<std::min(n, sms * 8), EscSmall::kThreads, smem, s>>>(g, list, n);
+                k_esc_rows<EscSmall, kNum, T><<<std::min(n, sms * 8), EscSmall::kThreads, smem, s>>>(
+                    g, list, n, &h->info->next[kNum][c]);
                 break;
             }
             case kClsE2: {
                 const size_t smem = kNum ? EscLarge::kNumericSmem : EscLarge::kSymbolicSmem;
-                k_esc_rows<EscLarge, kNum, T><<<std::min(n, sms), EscLarge::kThreads, smem, s>>>(g, list, n);
+                k_esc_rows<EscLarge, kNum, T><<<std::min(n, sms), EscLarge::kThreads, smem, s>>>(
+                    g, list, n, &h->info->next[kNum][c]);
                 break;
             }
             case kClsD: {
@@ -279,8 +222,8 @@ int run_symbolic(ops_handle_s *h, const Mat &A, const Mat &B, int *c_rpt, long l
     OPS_CUDA(h, cudaMemsetAsync(c_rpt + M, 0, sizeof(int), st));
     if (h->timing) OPS_CUDA(h, cudaEventRecord(h->ev_t[1], st));
     if (M > 0) {
-        k_setup<<<(M + kSetupThreads - 1) / kSetupThreads, kSetupThreads, 0, st>>>(A.rpt, A.col, B.rpt, M, A.cols,
-                                                                                 h->row_flop, h->lists, c_rpt, h->info);
+        k_setup<<<(M + kSetupThreads - 1) / kSetupThreads, kSetupThreads, 0, st>>>(
+            A.rpt, A.col, B.rpt, B.col, M, A.cols, B.cols, h->row_flop, h->lists, c_rpt, h->info);
         OPS_CUDA(h, cudaGetLastError());
         ++h->launches;
     }
@@ -338,6 +281,7 @@ int run_numeric(ops_handle_s *h, const Mat &A, const Mat &B, const int *c_rpt, i
         return fail(h, OPS_NOT_SUPPORTED, "numeric phase without a matching symbolic phase on this handle");
     if (h->counts[kClsD] > 0) OPS_CHECK(ensure_dense(h, B.cols, h->counts[kClsD], st));
     OPS_CUDA(h, cudaMemsetAsync(&h->info->flags, 0, sizeof(int), st));
+    OPS_CUDA(h, cudaMemsetAsync(h->info->next[1], 0, sizeof(h->info->next[1]), st));
     SpgemmArgs<T> g{};
     g.arpt = A.rpt;
     g.acol = A.col;
