@@ -320,7 +320,9 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="web", choices=["web", "laplacian", "stencil27", "stencil27_f32"])
+    ap.add_argument("--workload", default="web",
+                    choices=["web", "laplacian", "stencil27", "stencil27_f32", "batched", "backward", "backward_f32"])
+    ap.add_argument("--batch", type=int, default=4096, help="problems in the batched workload")
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
@@ -336,16 +338,169 @@ def main():
         if torch.cuda.is_available():
             torch.cuda.set_device(local_rank)
         dist.init_process_group(backend=backend)
-    desc, dt, data, n = make_workload(args.workload)
-    if args.impl == "reference":
-        run_reference(args, desc, dt, data, n, rank, world)
+    if args.workload == "batched":
+        run_batched(args, rank, world, local_rank)
+    elif args.workload.startswith("backward"):
+        run_backward(args, rank, world, local_rank)
     else:
-        run_ours(args, desc, dt, data, n, rank, world, local_rank)
+        desc, dt, data, n = make_workload(args.workload)
+        run_plain(args, desc, dt, data, n, rank, world, local_rank)
     if world > 1:
         import torch.distributed as dist
 
         dist.barrier()
         dist.destroy_process_group()
+
+
+def run_plain(args, desc, dt, data, n, rank, world, local_rank):
+    if args.impl == "reference":
+        run_reference(args, desc, dt, data, n, rank, world)
+    else:
+        run_ours(args, desc, dt, data, n, rank, world, local_rank)
+
+
+# ------------------------------------------------------------------- batched workload
+def run_batched(args, rank, world, local_rank):
+    """4,096 independent FP32 Erdos-Renyi products (sizes log-uniform in 64..65,536, mean
+    degree U(4,32)): per-call loop of ops_spgemm vs one planned batch (ops_batch_create +
+    ops_batch_execute) and vs graph replays of the planned numeric phase."""
+    import torch
+
+    import opsparse_gb300 as ops
+    from opsparse_gb300 import capi, gen_device
+
+    torch.cuda.set_device(local_rank)
+    if args.impl == "reference":
+        if rank == 0:
+            print(json.dumps({"metric": METRIC, "impl": "reference", "unavailable":
+                              "OpSparse has no batched SpGEMM and no CPU SpGEMM; see the plain workloads"}))
+        return
+    sizes, row_base, a_side, b_side = gen_device.er_batch(args.batch, dtype=torch.float32)
+    A = gen_device.problem_slices(sizes, row_base, a_side)
+    B = gen_device.problem_slices(sizes, row_base, b_side)
+    pairs = []
+    for (ar, ac, av, an), (br, bc, bv, bn), n in zip(A, B, sizes):
+        pairs.append((ops.CsrMatrix(int(n), int(n), ar, ac, av), ops.CsrMatrix(int(n), int(n), br, bc, bv)))
+    lib = capi.load()
+    h = ops.Handle()
+    stream = torch.cuda.Stream()
+    st = C.c_void_p(stream.cuda_stream)
+
+    def loop_once():
+        for Ap, Bp in pairs:
+            a, b = Ap.ptrs(), Bp.ptrs()
+            rp, cp, vp, nz = C.c_void_p(), C.c_void_p(), C.c_void_p(), C.c_int64()
+            capi.check(lib.ops_spgemm(h.h, capi.OPS_F32, Ap.rows, Ap.cols, Bp.cols, a[0], a[1], a[2], Ap.nnz, b[0],
+                                      b[1], b[2], Bp.nnz, C.byref(rp), C.byref(cp), C.byref(vp), C.byref(nz), st),
+                       h.h)
+            for p_ in (rp, cp, vp):
+                lib.ops_free(p_, st)
+
+    def timed(fn, reps):
+        ts = []
+        for _ in range(reps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            e0.record(stream)
+            fn()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ts.append(e0.elapsed_time(e1))
+        return float(np.median(ts))
+
+    with torch.cuda.stream(stream):
+        loop_once()  # warm-up
+        loop_ms = timed(loop_once, max(1, args.steps // 4))
+        holder = {}
+
+        def batched_full():
+            if "b" in holder:
+                holder["b"].close()
+            holder["b"] = ops.Batch(h, pairs, stream=stream)
+            holder["b"].execute(False)
+
+        batched_full()
+        full_ms = timed(batched_full, max(1, args.steps // 4))
+        bt = holder["b"]
+        bt.execute(True)  # records the graph
+        replay_ms = timed(lambda: bt.execute(True), args.steps)
+    seg, flop, nnz = bt.info()
+    gf = 2.0 * flop / (full_ms * 1e-3) / 1e9
+    line = {"metric": METRIC, "value": gf, "unit": "GFLOPS", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": full_ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (device-generated Erdos-Renyi pairs)",
+            "config": {"workload": f"batched_er_{args.batch}", "problems": args.batch, "sizes": "log-uniform 64..65536",
+                       "mean_degree": "U(4,32)", "values": "N(0,1)", "products": flop, "nnz_c": nnz,
+                       "segments": seg},
+            "batched": {"loop_ms": loop_ms, "batched_ms": full_ms, "speedup_vs_loop": loop_ms / full_ms,
+                        "graph_replay_numeric_ms": replay_ms}}
+    bt.close()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+# ----------------------------------------------------------------- backward workload
+def run_backward(args, rank, world, local_rank):
+    """C = A*B with A 200,000^2 power-law (mean degree 16, exponent 2.2) and B = pattern of
+    A^T with fresh values; loss = sum(W .* C).  Times the forward (numeric phase on the
+    fixed pattern, and the full SpGEMM) and forward + backward (dA, dB)."""
+    import torch
+
+    import opsparse_gb300 as ops
+    from opsparse_gb300 import gen
+    from opsparse_gb300.autograd import FixedPatternSpGEMM
+
+    torch.cuda.set_device(local_rank)
+    if args.impl == "reference":
+        if rank == 0:
+            print(json.dumps({"metric": METRIC, "impl": "reference", "unavailable":
+                              "OpSparse has no backward pass; see the plain workloads"}))
+        return
+    dt = torch.float32 if args.workload.endswith("f32") else torch.float64
+    n = 200_000
+    a = gen.powerlaw_square(n, 16, 2.2)
+    b = gen.transpose_pattern(a[0], a[1], n)
+    A = ops.csr_to_device(*a, n, n, dtype=dt)
+    B = ops.csr_to_device(*b, n, n, dtype=dt)
+    h = ops.Handle()
+    op = FixedPatternSpGEMM(A, B, h)
+    w = torch.randn(op.nnz, dtype=dt, device="cuda")
+    flop = int(gen.row_flop(a[0], a[1], b[0]).sum())
+
+    def timed(fn, reps):
+        ts = []
+        for _ in range(reps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            e0.record()
+            fn()
+            e1.record()
+            torch.cuda.synchronize()
+            ts.append(e0.elapsed_time(e1))
+        return float(np.median(ts))
+
+    fwd = lambda: op.forward_values(A.val, B.val)  # noqa: E731
+    fwdbwd = lambda: (op.forward_values(A.val, B.val), op.backward_values(A.val, B.val, w))  # noqa: E731
+    full = lambda: h.spgemm_oneshot(A, B)  # noqa: E731
+    for _ in range(max(args.warmup, 3)):
+        fwdbwd()
+        full()
+    fwd_ms = timed(fwd, args.steps)
+    fwdbwd_ms = timed(fwdbwd, args.steps)
+    full_ms = timed(full, args.steps)
+    products, with_map = op.plan_info()
+    line = {"metric": METRIC, "value": 2.0 * flop / (fwdbwd_ms * 1e-3) / 1e9, "unit": "GFLOPS", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": fwdbwd_ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64" if dt == torch.float64 else "f32",
+            "data": "synthetic", "config": {"workload": "powerlaw_200k_AAt_fwd_bwd", "rows": n, "mean_degree": 16,
+                                            "exponent": 2.2, "products": flop, "nnz_c": op.nnz},
+            "fwd_bwd": {"forward_numeric_ms": fwd_ms, "forward_full_ms": full_ms, "fwd_bwd_ms": fwdbwd_ms,
+                        "ratio_vs_numeric_forward": fwdbwd_ms / fwd_ms,
+                        "ratio_vs_full_forward": (fwdbwd_ms - fwd_ms + full_ms) / full_ms,
+                        "product_map": with_map}}
+    h.close()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
 
 
 if __name__ == "__main__":

@@ -85,6 +85,12 @@ int ops_handle_set_dense_budget(ops_handle_t handle, size_t bytes);
  * with ops_free; 1 = cudaMalloc, release with cudaFree (what OpSparse's CSR::drelease
  * expects). */
 int ops_handle_set_output_malloc(ops_handle_t handle, int use_cuda_malloc);
+/* Row-class thresholds used by the next symbolic phase, as 6 int32 upper bounds on a
+ * row's intermediate products: {R8, R16, R32, W, E1, E2} (defaults {8, 16, 32, 128, 1024,
+ * 13312}, which are also the maxima; 0 switches a class off; rows above E2 use the dense
+ * class).  Replaces OpSparse's compile-time bin ranges (kernels/binning.cuh:21,105). */
+int ops_handle_set_thresholds(ops_handle_t handle, const int32_t *thresholds, int count);
+int ops_handle_get_thresholds(ops_handle_t handle, int32_t *thresholds, int count);
 /* Message for the last failing call on this handle ("" if none). */
 const char *ops_handle_last_error(ops_handle_t handle);
 const char *ops_status_string(int status);
@@ -140,6 +146,51 @@ int ops_spgemm_backward(ops_handle_t handle, int dtype, int32_t rows_a, int32_t 
 int ops_handle_set_map_budget(ops_handle_t handle, size_t bytes);
 /* Products and map mode (1 = map kept) of the current backward plan. */
 int ops_backward_plan_info(ops_handle_t handle, int64_t *products, int *with_map);
+
+/* ------------------------------------------------------------------- batched -- */
+/* Many independent products C_b = A_b * B_b (no counterpart in OpSparse).  Each item holds
+ * device CSR arrays; A_b is rows x cols_a, B_b is cols_a x cols_b. */
+typedef struct {
+    int32_t rows, cols_a, cols_b;
+    int64_t a_nnz, b_nnz;
+    const int32_t *a_rpt, *a_col;
+    const void *a_val;
+    const int32_t *b_rpt, *b_col;
+    const void *b_val;
+} ops_batch_item;
+
+typedef struct ops_batch_s *ops_batch_t;
+
+/* Plans a batch: per-problem product counts, grouping into segments whose products fit
+ * int32, block-diagonal layout of each segment, one row classification per segment over
+ * all its problems, symbolic phase, scan, and allocation of every C_b.  The items' value
+ * pointers are read by ops_batch_execute, which may be called repeatedly with new values
+ * in the same arrays.  The handle's row-class thresholds are used.  Synchronizes. */
+int ops_batch_create(ops_handle_t handle, int dtype, int32_t count, const ops_batch_item *items, ops_batch_t *batch,
+                     void *stream);
+/* Numeric phase of every problem.  use_graph = 1: the first call records the work on
+ * `stream` (a created stream) as a CUDA graph and later calls replay it with a single
+ * cudaGraphLaunch; use_graph = 0: plain launches.  Asynchronous. */
+int ops_batch_execute(ops_batch_t batch, int use_graph, void *stream);
+/* Device-side error flags of the last execute (synchronizes). */
+int ops_batch_check(ops_batch_t batch, void *stream);
+/* Device pointers of C_b (views into the batch's storage, valid until destroy). */
+int ops_batch_result(ops_batch_t batch, int32_t index, int32_t **c_rpt, int32_t **c_col, void **c_val,
+                     int64_t *c_nnz);
+int ops_batch_info(ops_batch_t batch, int32_t *segments, int64_t *flop, int64_t *nnz);
+int ops_batch_destroy(ops_batch_t batch);
+
+/* ----------------------------------------------------------------- autotuner -- */
+/* Chooses the row-class thresholds (see ops_handle_set_thresholds) for a workload by
+ * coordinate descent, timing complete batched runs of `items` (a representative sample)
+ * with CUDA events, median of `reps` runs per candidate.  Installs the best thresholds on
+ * the handle and returns them in best[6] (and the time in *best_ms).  Synchronizes. */
+int ops_autotune(ops_handle_t handle, int dtype, int32_t count, const ops_batch_item *items, int reps,
+                 int32_t *best, float *best_ms, void *stream);
+/* Tuning records persisted as JSON {"<key>": [6 thresholds], ...}; key typically names the
+ * GPU and the workload.  lookup returns OPS_NOT_SUPPORTED when the key is absent. */
+int ops_tuning_store(const char *path, const char *key, const int32_t *thresholds);
+int ops_tuning_lookup(const char *path, const char *key, int32_t *thresholds);
 
 /* Per-row intermediate-product counts (row_flop, rows_a int64, device; may be NULL) and
  * their sum (*total, host).  Synchronizes the stream. */

@@ -107,6 +107,15 @@ class Handle:
     def set_timing(self, level: int):
         check(self.lib.ops_handle_set_timing(self.h, int(level)), self.h)
 
+    def set_thresholds(self, th):
+        arr = (C.c_int32 * 6)(*[int(x) for x in th])
+        check(self.lib.ops_handle_set_thresholds(self.h, arr, 6), self.h)
+
+    def get_thresholds(self):
+        arr = (C.c_int32 * 6)()
+        check(self.lib.ops_handle_get_thresholds(self.h, arr, 6), self.h)
+        return list(arr)
+
     def set_dense_budget(self, nbytes: int):
         check(self.lib.ops_handle_set_dense_budget(self.h, int(nbytes)), self.h)
 
@@ -183,3 +192,101 @@ def flop(A: CsrMatrix, B: CsrMatrix, stream=None) -> int:
     check(lib.ops_flop(A.rows, A.cols, A.rpt.data_ptr(), A.col.data_ptr() if A.nnz else None, B.rpt.data_ptr(),
                        None, C.byref(tot), _stream_ptr(stream)))
     return int(tot.value)
+
+
+class Batch:
+    """Many independent products C_b = A_b * B_b planned once (ops_batch_create) and
+    executed repeatedly (ops_batch_execute, optionally as one CUDA-graph launch)."""
+
+    def __init__(self, handle: Handle, pairs, stream=None):
+        torch = _torch()
+        self.h = handle
+        self.lib = handle.lib
+        self.pairs = pairs  # keep the device arrays alive
+        n = len(pairs)
+        items = (capi.BatchItem * max(n, 1))()
+        self.dtype = pairs[0][0].val.dtype if n else torch.float64
+        for i, (A, B) in enumerate(pairs):
+            a, b = A.ptrs(), B.ptrs()
+            items[i] = capi.BatchItem(A.rows, A.cols, B.cols, A.nnz, B.nnz, a[0], a[1], a[2], b[0], b[1], b[2])
+        out = C.c_void_p()
+        self.stream = stream or torch.cuda.Stream()
+        check(self.lib.ops_batch_create(handle.h, _dtype_code(torch.empty(0, dtype=self.dtype)), n, items,
+                                        C.byref(out), C.c_void_p(self.stream.cuda_stream)), handle.h)
+        self.b = out
+        self.n = n
+
+    def execute(self, use_graph: bool = True):
+        check(self.lib.ops_batch_execute(self.b, 1 if use_graph else 0, C.c_void_p(self.stream.cuda_stream)),
+              self.h.h)
+
+    def check(self):
+        check(self.lib.ops_batch_check(self.b, C.c_void_p(self.stream.cuda_stream)), self.h.h)
+
+    def info(self):
+        seg, fl, nz = C.c_int32(0), C.c_int64(0), C.c_int64(0)
+        check(self.lib.ops_batch_info(self.b, C.byref(seg), C.byref(fl), C.byref(nz)))
+        return int(seg.value), int(fl.value), int(nz.value)
+
+    def result(self, i: int):
+        """(rpt, col, val) numpy copies of C_i."""
+        torch = _torch()
+        rp, cp, vp, nnz = C.c_void_p(), C.c_void_p(), C.c_void_p(), C.c_int64(0)
+        check(self.lib.ops_batch_result(self.b, i, C.byref(rp), C.byref(cp), C.byref(vp), C.byref(nnz)), self.h.h)
+        A = self.pairs[i][0]
+        n = int(nnz.value)
+        self.stream.synchronize()
+        rpt = torch.as_tensor(_DevArray(rp.value, A.rows + 1, "<i4"), device="cuda").cpu().numpy()
+        if n == 0:
+            return rpt, np_empty("i4"), np_empty("f8" if self.dtype == torch.float64 else "f4")
+        col = torch.as_tensor(_DevArray(cp.value, n, "<i4"), device="cuda").cpu().numpy()
+        val = torch.as_tensor(_DevArray(vp.value, n, "<f8" if self.dtype == torch.float64 else "<f4"),
+                              device="cuda").cpu().numpy()
+        return rpt, col, val
+
+    def close(self):
+        if getattr(self, "b", None):
+            self.lib.ops_batch_destroy(self.b)
+            self.b = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def np_empty(kind: str):
+    import numpy as np
+
+    return np.zeros(0, dtype=kind)
+
+
+def batch_items(pairs):
+    items = (capi.BatchItem * max(len(pairs), 1))()
+    for i, (A, B) in enumerate(pairs):
+        a, b = A.ptrs(), B.ptrs()
+        items[i] = capi.BatchItem(A.rows, A.cols, B.cols, A.nnz, B.nnz, a[0], a[1], a[2], b[0], b[1], b[2])
+    return items
+
+
+def autotune(handle: Handle, pairs, reps: int = 3, stream=None):
+    """Runs the library's autotuner on (a sample of) a workload; returns (thresholds, ms)."""
+    torch = _torch()
+    best = (C.c_int32 * 6)()
+    ms = C.c_float(0)
+    st = stream or torch.cuda.Stream()
+    check(handle.lib.ops_autotune(handle.h, _dtype_code(pairs[0][0].val), len(pairs), batch_items(pairs), reps, best,
+                                  C.byref(ms), C.c_void_p(st.cuda_stream)), handle.h)
+    return list(best), float(ms.value)
+
+
+def tuning_store(path: str, key: str, thresholds) -> None:
+    arr = (C.c_int32 * 6)(*[int(x) for x in thresholds])
+    check(load().ops_tuning_store(str(path).encode(), key.encode(), arr))
+
+
+def tuning_lookup(path: str, key: str):
+    arr = (C.c_int32 * 6)()
+    st = load().ops_tuning_lookup(str(path).encode(), key.encode(), arr)
+    return list(arr) if st == capi.OPS_OK else None

@@ -60,6 +60,11 @@ class Timings(C.Structure):
         return d
 
 
+class BatchItem(C.Structure):
+    _fields_ = [("rows", I32), ("cols_a", I32), ("cols_b", I32), ("a_nnz", I64), ("b_nnz", I64),
+                ("a_rpt", P), ("a_col", P), ("a_val", P), ("b_rpt", P), ("b_col", P), ("b_val", P)]
+
+
 _SIGS = {
     "ops_version": (C.c_char_p, []),
     "ops_status_string": (C.c_char_p, [C.c_int]),
@@ -69,6 +74,8 @@ _SIGS = {
     "ops_handle_get_timings": (C.c_int, [P, C.POINTER(Timings)]),
     "ops_handle_set_dense_budget": (C.c_int, [P, C.c_size_t]),
     "ops_handle_set_output_malloc": (C.c_int, [P, C.c_int]),
+    "ops_handle_set_thresholds": (C.c_int, [P, C.POINTER(I32), C.c_int]),
+    "ops_handle_get_thresholds": (C.c_int, [P, C.POINTER(I32), C.c_int]),
     "ops_handle_last_error": (C.c_char_p, [P]),
     "ops_spgemm": (C.c_int, [P, C.c_int, I32, I32, I32, P, P, P, I64, P, P, P, I64,
                              C.POINTER(P), C.POINTER(P), C.POINTER(P), C.POINTER(I64), P]),
@@ -81,6 +88,15 @@ _SIGS = {
     "ops_spgemm_backward": (C.c_int, [P, C.c_int, I32, I32, I32, P, P, P, I64, P, P, P, I64, P, P, P, P, P, P]),
     "ops_handle_set_map_budget": (C.c_int, [P, C.c_size_t]),
     "ops_backward_plan_info": (C.c_int, [P, C.POINTER(I64), C.POINTER(C.c_int)]),
+    "ops_batch_create": (C.c_int, [P, C.c_int, I32, C.POINTER(BatchItem), C.POINTER(P), P]),
+    "ops_batch_execute": (C.c_int, [P, C.c_int, P]),
+    "ops_batch_check": (C.c_int, [P, P]),
+    "ops_batch_result": (C.c_int, [P, I32, C.POINTER(P), C.POINTER(P), C.POINTER(P), C.POINTER(I64)]),
+    "ops_batch_info": (C.c_int, [P, C.POINTER(I32), C.POINTER(I64), C.POINTER(I64)]),
+    "ops_batch_destroy": (C.c_int, [P]),
+    "ops_autotune": (C.c_int, [P, C.c_int, I32, C.POINTER(BatchItem), C.c_int, C.POINTER(I32), C.POINTER(C.c_float), P]),
+    "ops_tuning_store": (C.c_int, [C.c_char_p, C.c_char_p, C.POINTER(I32)]),
+    "ops_tuning_lookup": (C.c_int, [C.c_char_p, C.c_char_p, C.POINTER(I32)]),
 }
 
 

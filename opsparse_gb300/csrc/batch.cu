@@ -1,0 +1,617 @@
+// batch.cu — many independent SpGEMMs C_b = A_b * B_b in one pass (no counterpart in
+// OpSparse).
+//
+// Problems are grouped into segments whose total intermediate products (an upper bound on
+// nnz(C)) fit int32.  Each segment is laid out on the device as one block-diagonal
+// product: A_seg stacks the A_b with their columns shifted to select the B_b rows, and
+// B_seg stacks the B_b with their own (local) columns.  A row of A_seg only reaches its
+// own problem's rows of B_seg, so C_seg is the stack of the C_b, with local columns.  One
+// row classification then covers every row of every problem in the segment (a global bin
+// queue per row class), and the single-matrix kernels run unchanged on it.
+//
+// ops_batch_create runs the flop count, segmentation, gather, classification, symbolic
+// phase and scan of every segment, and allocates all outputs.  ops_batch_execute runs the
+// numeric phase of all segments (re-gathering A's and B's values, which may change between
+// calls): the first call records it on the stream as a CUDA graph, later calls replay that
+// graph with one cudaGraphLaunch.
+#include <algorithm>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <new>
+#include <vector>
+
+#include "common.cuh"
+#include "internal.hpp"
+
+using namespace opsg;
+using namespace opsg_internal;
+
+namespace {
+
+struct Item {  // device copy of an ops_batch_item plus its placement in its segment
+    int rows, cols_a, cols_b;
+    long long a_nnz, b_nnz;
+    const int *a_rpt, *a_col;
+    const void *a_val;
+    const int *b_rpt, *b_col;
+    const void *b_val;
+    int row_base;       // first row of the problem in its segment's A_seg / C_seg
+    int k_base;         // first row of the problem's B block in B_seg
+    long long a_base;   // first entry of the problem in A_seg
+    long long b_base;   // first entry of the problem in B_seg
+    long long c_rpt_base;  // first entry of the problem's rebased row_ptr in the result arena
+};
+
+struct Segment {
+    int first, count;   // problems [first, first + count)
+    int M, K, N;        // A_seg is M x K, B_seg is K x N
+    long long a_nnz, b_nnz, flop;
+    int *a_rpt = nullptr, *a_col = nullptr, *b_rpt = nullptr, *b_col = nullptr;
+    void *a_val = nullptr, *b_val = nullptr;
+    int *c_rpt = nullptr, *c_col = nullptr;
+    void *c_val = nullptr;
+    long long c_nnz = 0;
+    ops_handle_s *h = nullptr;  // per-segment plan (classes, workspace)
+};
+
+// per-problem intermediate products: one CTA per problem
+__global__ void k_batch_flop(const Item *__restrict__ items, int n, unsigned long long *__restrict__ flop)
+{
+    for (int b = blockIdx.x; b < n; b += gridDim.x) {
+        const Item it = items[b];
+        unsigned long long s = 0;
+        for (int r = threadIdx.x; r < it.rows; r += blockDim.x) {
+            for (int p = it.a_rpt[r]; p < it.a_rpt[r + 1]; ++p) {
+                const int j = it.a_col[p];
+                if ((unsigned)j < (unsigned)it.cols_a) s += (unsigned long long)(it.b_rpt[j + 1] - it.b_rpt[j]);
+            }
+        }
+#pragma unroll
+        for (int d = 16; d >= 1; d >>= 1) s += __shfl_xor_sync(kFull, s, d);
+        __shared__ unsigned long long part[32];
+        if (lane_id() == 0) part[threadIdx.x >> 5] = s;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            unsigned long long t = 0;
+            for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += part[w];
+            flop[b] = t;
+        }
+        __syncthreads();
+    }
+}
+
+// Builds one segment's block-diagonal structure (rpt, col); one CTA per problem.
+__global__ void k_batch_gather_structure(const Item *__restrict__ items, int first, int count, int *a_rpt, int *a_col,
+                                         int *b_rpt, int *b_col)
+{
+    for (int b = blockIdx.x; b < count; b += gridDim.x) {
+        const Item it = items[first + b];
+        for (int r = threadIdx.x; r < it.rows; r += blockDim.x) a_rpt[it.row_base + r] = (int)(it.a_base + it.a_rpt[r]);
+        for (long long p = threadIdx.x; p < it.a_nnz; p += blockDim.x) a_col[it.a_base + p] = it.a_col[p] + it.k_base;
+        for (int r = threadIdx.x; r < it.cols_a; r += blockDim.x) b_rpt[it.k_base + r] = (int)(it.b_base + it.b_rpt[r]);
+        for (long long p = threadIdx.x; p < it.b_nnz; p += blockDim.x) b_col[it.b_base + p] = it.b_col[p];
+    }
+}
+
+template <typename T>
+__global__ void k_batch_gather_values(const Item *__restrict__ items, int first, int count, T *a_val, T *b_val)
+{
+    for (int b = blockIdx.x; b < count; b += gridDim.x) {
+        const Item it = items[first + b];
+        const T *av = static_cast<const T *>(it.a_val);
+        const T *bv = static_cast<const T *>(it.b_val);
+        for (long long p = threadIdx.x; p < it.a_nnz; p += blockDim.x) a_val[it.a_base + p] = av[p];
+        for (long long p = threadIdx.x; p < it.b_nnz; p += blockDim.x) b_val[it.b_base + p] = bv[p];
+    }
+}
+
+// Per-problem row_ptr rebased to start at 0, written to the result arena.
+__global__ void k_batch_rebase(const Item *__restrict__ items, int first, int count, const int *__restrict__ c_rpt,
+                               int *out)
+{
+    for (int b = blockIdx.x; b < count; b += gridDim.x) {
+        const Item it = items[first + b];
+        const int base = c_rpt[it.row_base];
+        for (int r = threadIdx.x; r <= it.rows; r += blockDim.x) out[it.c_rpt_base + r] = c_rpt[it.row_base + r] - base;
+    }
+}
+
+}  // namespace
+
+struct ops_batch_s {
+    ops_handle_s *owner = nullptr;
+    int dtype = OPS_F64;
+    int n = 0;
+    std::vector<Item> items;     // host copy
+    Item *d_items = nullptr;
+    std::vector<Segment> segs;
+    int *c_rpt_arena = nullptr;  // all rebased per-problem row pointers
+    void *mem = nullptr;         // one pool allocation for inputs and outputs of all segments
+    long long flop = 0, nnz = 0;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    cudaStream_t graph_stream = nullptr;
+};
+
+extern "C" int ops_spgemm_symbolic(ops_handle_t, int32_t, int32_t, int32_t, const int32_t *, const int32_t *, int64_t,
+                                   const int32_t *, const int32_t *, int64_t, int32_t *, int64_t *, void *);
+extern "C" int ops_spgemm_numeric(ops_handle_t, int, int32_t, int32_t, int32_t, const int32_t *, const int32_t *,
+                                  const void *, const int32_t *, const int32_t *, const void *, const int32_t *,
+                                  int32_t *, void *, void *);
+
+namespace {
+
+void batch_release(ops_batch_s *b)
+{
+    if (!b) return;
+    cudaDeviceSynchronize();
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    if (b->graph) cudaGraphDestroy(b->graph);
+    for (Segment &s : b->segs) {
+        if (s.h) ops_handle_destroy(s.h);
+        if (s.c_col) cudaFree(s.c_col);
+        if (s.c_val) cudaFree(s.c_val);
+    }
+    if (b->mem) cudaFree(b->mem);
+    if (b->d_items) cudaFree(b->d_items);
+    (void)cudaGetLastError();
+    delete b;
+}
+
+size_t seg_bytes(const Segment &s, size_t vs)
+{
+    return align_up(4 * ((size_t)s.M + 1), 256) + align_up(4 * (size_t)std::max(1LL, s.a_nnz), 256) +
+           align_up(vs * (size_t)std::max(1LL, s.a_nnz), 256) + align_up(4 * ((size_t)s.K + 1), 256) +
+           align_up(4 * (size_t)std::max(1LL, s.b_nnz), 256) + align_up(vs * (size_t)std::max(1LL, s.b_nnz), 256) +
+           align_up(4 * ((size_t)s.M + 1), 256);
+}
+
+}  // namespace
+
+extern "C" int ops_batch_create(ops_handle_t h, int dtype, int32_t count, const ops_batch_item *items,
+                                ops_batch_t *out, void *stream)
+{
+    if (!h || !out || count < 0 || (count > 0 && !items)) return OPS_INVALID_ARGUMENT;
+    if (dtype != OPS_F64 && dtype != OPS_F32) return fail(h, OPS_INVALID_ARGUMENT, "unknown dtype");
+    *out = nullptr;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const size_t vs = dtype == OPS_F64 ? 8 : 4;
+    ops_batch_s *b = new (std::nothrow) ops_batch_s();
+    if (!b) return OPS_EXCEPTION;
+    b->owner = h;
+    b->dtype = dtype;
+    b->n = count;
+    b->items.resize(count);
+    for (int i = 0; i < count; ++i) {
+        const ops_batch_item &s = items[i];
+        if (s.rows < 0 || s.cols_a < 0 || s.cols_b < 0 || s.a_nnz < 0 || s.b_nnz < 0 || (s.rows > 0 && !s.a_rpt) ||
+            (s.cols_a > 0 && !s.b_rpt) || (s.a_nnz > 0 && (!s.a_col || !s.a_val)) ||
+            (s.b_nnz > 0 && (!s.b_col || !s.b_val))) {
+            batch_release(b);
+            return fail(h, OPS_INVALID_ARGUMENT, "bad batch item " + std::to_string(i));
+        }
+        Item &it = b->items[i];
+        it.rows = s.rows;
+        it.cols_a = s.cols_a;
+        it.cols_b = s.cols_b;
+        it.a_nnz = s.a_nnz;
+        it.b_nnz = s.b_nnz;
+        it.a_rpt = s.a_rpt;
+        it.a_col = s.a_col;
+        it.a_val = s.a_val;
+        it.b_rpt = s.b_rpt;
+        it.b_col = s.b_col;
+        it.b_val = s.b_val;
+    }
+    auto bail = [&](int status) {
+        batch_release(b);
+        return status;
+    };
+    // 1. per-problem products (device), then segmentation on the host
+    std::vector<unsigned long long> flop(std::max(count, 1), 0ull);
+    {
+        void *p = nullptr;
+        cudaError_t e = cudaMalloc(&p, sizeof(Item) * std::max(count, 1));
+        if (e != cudaSuccess) return bail(fail(h, status_of(e), "allocating batch descriptors"));
+        b->d_items = static_cast<Item *>(p);
+        void *f = nullptr;
+        e = cudaMallocAsync(&f, sizeof(unsigned long long) * std::max(count, 1), st);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(b->d_items, b->items.data(), sizeof(Item) * count, cudaMemcpyHostToDevice, st);
+        if (e == cudaSuccess && count > 0) {
+            k_batch_flop<<<std::min(count, 65535), 256, 0, st>>>(b->d_items, count, static_cast<unsigned long long *>(f));
+            e = cudaGetLastError();
+        }
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(flop.data(), f, sizeof(unsigned long long) * count, cudaMemcpyDeviceToHost, st);
+        if (f) cudaFreeAsync(f, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) {
+            (void)cudaGetLastError();
+            return bail(fail(h, status_of(e), std::string("batch flop count: ") + cudaGetErrorString(e)));
+        }
+    }
+    const long long kLimit = 0x7fff0000LL;  // products (>= nnz(C)), rows and nnz per segment stay in int32
+    int first = 0;
+    while (first < count) {
+        Segment s{};
+        s.first = first;
+        long long M = 0, K = 0, an = 0, bn = 0, fl = 0;
+        int N = 0, i = first;
+        for (; i < count; ++i) {
+            const Item &it = b->items[i];
+            const long long f = (long long)flop[i];
+            if (i > first && (fl + f > kLimit || M + it.rows > kLimit || K + it.cols_a > kLimit ||
+                              an + it.a_nnz > kLimit || bn + it.b_nnz > kLimit))
+                break;
+            if (f > kLimit || it.a_nnz > kLimit || it.b_nnz > kLimit)
+                return bail(fail(h, OPS_INT32_OVERFLOW, "a batch item exceeds the int32 limits of one product"));
+            Item &w = b->items[i];
+            w.row_base = (int)M;
+            w.k_base = (int)K;
+            w.a_base = an;
+            w.b_base = bn;
+            M += it.rows;
+            K += it.cols_a;
+            an += it.a_nnz;
+            bn += it.b_nnz;
+            fl += f;
+            N = std::max(N, it.cols_b);
+        }
+        s.count = i - first;
+        s.M = (int)M;
+        s.K = (int)K;
+        s.N = N;
+        s.a_nnz = an;
+        s.b_nnz = bn;
+        s.flop = fl;
+        b->flop += fl;
+        b->segs.push_back(s);
+        first = i;
+    }
+    // result row_ptr offsets
+    long long rb = 0;
+    for (Item &it : b->items) {
+        it.c_rpt_base = rb;
+        rb += it.rows + 1;
+    }
+    // 2. one allocation for every segment's inputs and row pointers plus the rebased arena
+    size_t total = align_up(4 * (size_t)std::max(1LL, rb), 256);
+    for (const Segment &s : b->segs) total += seg_bytes(s, vs);
+    {
+        cudaError_t e = cudaMalloc(&b->mem, total);
+        if (e != cudaSuccess) return bail(fail(h, status_of(e), "allocating batch arena"));
+        e = cudaMemcpyAsync(b->d_items, b->items.data(), sizeof(Item) * count, cudaMemcpyHostToDevice, st);
+        if (e != cudaSuccess) return bail(fail(h, status_of(e), "copying batch descriptors"));
+    }
+    unsigned char *m = static_cast<unsigned char *>(b->mem);
+    b->c_rpt_arena = reinterpret_cast<int *>(m);
+    m += align_up(4 * (size_t)std::max(1LL, rb), 256);
+    for (Segment &s : b->segs) {
+        s.a_rpt = reinterpret_cast<int *>(m);
+        m += align_up(4 * ((size_t)s.M + 1), 256);
+        s.a_col = reinterpret_cast<int *>(m);
+        m += align_up(4 * (size_t)std::max(1LL, s.a_nnz), 256);
+        s.a_val = m;
+        m += align_up(vs * (size_t)std::max(1LL, s.a_nnz), 256);
+        s.b_rpt = reinterpret_cast<int *>(m);
+        m += align_up(4 * ((size_t)s.K + 1), 256);
+        s.b_col = reinterpret_cast<int *>(m);
+        m += align_up(4 * (size_t)std::max(1LL, s.b_nnz), 256);
+        s.b_val = m;
+        m += align_up(vs * (size_t)std::max(1LL, s.b_nnz), 256);
+        s.c_rpt = reinterpret_cast<int *>(m);
+        m += align_up(4 * ((size_t)s.M + 1), 256);
+        // 3. structure, last row pointers, classification + symbolic + scan
+        const int last_a = (int)s.a_nnz, last_b = (int)s.b_nnz;
+        cudaError_t e = cudaMemcpyAsync(s.a_rpt + s.M, &last_a, sizeof(int), cudaMemcpyHostToDevice, st);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(s.b_rpt + s.K, &last_b, sizeof(int), cudaMemcpyHostToDevice, st);
+        if (e == cudaSuccess && s.count > 0) {
+            k_batch_gather_structure<<<std::min(s.count, 65535), 256, 0, st>>>(b->d_items, s.first, s.count, s.a_rpt,
+                                                                              s.a_col, s.b_rpt, s.b_col);
+            e = cudaGetLastError();
+        }
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);  // host values above must outlive the copies
+        if (e != cudaSuccess) return bail(fail(h, status_of(e), std::string("batch gather: ") + cudaGetErrorString(e)));
+        int stt = ops_handle_create(&s.h);
+        if (stt != OPS_OK) return bail(fail(h, stt, "creating a segment handle"));
+        s.h->th = h->th;
+        int64_t nnz = 0;
+        stt = ops_spgemm_symbolic(s.h, s.M, s.K, s.N, s.a_rpt, s.a_col, s.a_nnz, s.b_rpt, s.b_col, s.b_nnz, s.c_rpt,
+                                  &nnz, st);
+        if (stt != OPS_OK) return bail(fail(h, stt, std::string("segment symbolic: ") + s.h->last_error));
+        s.c_nnz = nnz;
+        b->nnz += nnz;
+        void *cc = nullptr, *cv = nullptr;
+        e = cudaMalloc(&cc, 4 * (size_t)std::max<int64_t>(nnz, 1));
+        if (e == cudaSuccess) e = cudaMalloc(&cv, vs * (size_t)std::max<int64_t>(nnz, 1));
+        if (e != cudaSuccess) {
+            if (cc) cudaFree(cc);
+            return bail(fail(h, status_of(e), "allocating a segment's C"));
+        }
+        s.c_col = static_cast<int *>(cc);
+        s.c_val = cv;
+        if (s.count > 0) {
+            k_batch_rebase<<<std::min(s.count, 65535), 256, 0, st>>>(b->d_items, s.first, s.count, s.c_rpt,
+                                                                    b->c_rpt_arena);
+            e = cudaGetLastError();
+            if (e != cudaSuccess) return bail(fail(h, status_of(e), "rebasing row pointers"));
+        }
+    }
+    cudaError_t e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return bail(fail(h, status_of(e), "batch create"));
+    *out = b;
+    return OPS_OK;
+}
+
+namespace {
+
+int record_numeric(ops_batch_s *b, cudaStream_t st)
+{
+    ops_handle_s *h = b->owner;
+    for (Segment &s : b->segs) {
+        if (s.count == 0) continue;
+        if (b->dtype == OPS_F64)
+            k_batch_gather_values<double><<<std::min(s.count, 65535), 256, 0, st>>>(
+                b->d_items, s.first, s.count, static_cast<double *>(s.a_val), static_cast<double *>(s.b_val));
+        else
+            k_batch_gather_values<float><<<std::min(s.count, 65535), 256, 0, st>>>(
+                b->d_items, s.first, s.count, static_cast<float *>(s.a_val), static_cast<float *>(s.b_val));
+        OPS_CUDA(h, cudaGetLastError());
+        const int stt = ops_spgemm_numeric(s.h, b->dtype, s.M, s.K, s.N, s.a_rpt, s.a_col, s.a_val, s.b_rpt, s.b_col,
+                                           s.b_val, s.c_rpt, s.c_col, s.c_val, st);
+        if (stt != OPS_OK) return fail(h, stt, std::string("segment numeric: ") + s.h->last_error);
+    }
+    return OPS_OK;
+}
+
+}  // namespace
+
+extern "C" int ops_batch_execute(ops_batch_t b, int use_graph, void *stream)
+{
+    if (!b) return OPS_INVALID_ARGUMENT;
+    ops_handle_s *h = b->owner;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    if (!use_graph) return record_numeric(b, st);
+    if (b->exec && b->graph_stream == st) {
+        OPS_CUDA(h, cudaGraphLaunch(b->exec, st));
+        return OPS_OK;
+    }
+    if (!st) return fail(h, OPS_INVALID_ARGUMENT, "graph replay needs a created stream, not the legacy stream");
+    if (b->exec) {
+        cudaGraphExecDestroy(b->exec);
+        b->exec = nullptr;
+    }
+    if (b->graph) {
+        cudaGraphDestroy(b->graph);
+        b->graph = nullptr;
+    }
+    OPS_CUDA(h, cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    const int rec = record_numeric(b, st);
+    cudaGraph_t g = nullptr;
+    const cudaError_t ec = cudaStreamEndCapture(st, &g);
+    if (rec != OPS_OK) {
+        if (g) cudaGraphDestroy(g);
+        return rec;
+    }
+    if (ec != cudaSuccess) {
+        (void)cudaGetLastError();
+        return fail(h, status_of(ec), std::string("capturing the batch: ") + cudaGetErrorString(ec));
+    }
+    b->graph = g;
+    OPS_CUDA(h, cudaGraphInstantiate(&b->exec, g, 0));
+    b->graph_stream = st;
+    OPS_CUDA(h, cudaGraphLaunch(b->exec, st));
+    return OPS_OK;
+}
+
+extern "C" int ops_batch_check(ops_batch_t b, void *stream)
+{
+    if (!b) return OPS_INVALID_ARGUMENT;
+    for (Segment &s : b->segs) {
+        if (s.count == 0) continue;
+        const int stt = ops_spgemm_check(s.h, stream);
+        if (stt != OPS_OK) return fail(b->owner, stt, s.h->last_error);
+    }
+    return OPS_OK;
+}
+
+extern "C" int ops_batch_result(ops_batch_t b, int32_t index, int32_t **c_rpt, int32_t **c_col, void **c_val,
+                                int64_t *c_nnz)
+{
+    if (!b || index < 0 || index >= b->n || !c_rpt || !c_col || !c_val || !c_nnz) return OPS_INVALID_ARGUMENT;
+    const Item &it = b->items[index];
+    const Segment *seg = nullptr;
+    for (const Segment &s : b->segs)
+        if (index >= s.first && index < s.first + s.count) seg = &s;
+    if (!seg) return OPS_INVALID_ARGUMENT;
+    int base = 0, end = 0;
+    OPS_CUDA(b->owner, cudaMemcpy(&base, seg->c_rpt + it.row_base, sizeof(int), cudaMemcpyDeviceToHost));
+    OPS_CUDA(b->owner, cudaMemcpy(&end, seg->c_rpt + it.row_base + it.rows, sizeof(int), cudaMemcpyDeviceToHost));
+    const size_t vs = b->dtype == OPS_F64 ? 8 : 4;
+    *c_rpt = b->c_rpt_arena + it.c_rpt_base;
+    *c_col = seg->c_col + base;
+    *c_val = static_cast<unsigned char *>(seg->c_val) + vs * (size_t)base;
+    *c_nnz = end - base;
+    return OPS_OK;
+}
+
+extern "C" int ops_batch_info(ops_batch_t b, int32_t *segments, int64_t *flop, int64_t *nnz)
+{
+    if (!b) return OPS_INVALID_ARGUMENT;
+    if (segments) *segments = (int32_t)b->segs.size();
+    if (flop) *flop = b->flop;
+    if (nnz) *nnz = b->nnz;
+    return OPS_OK;
+}
+
+extern "C" int ops_batch_destroy(ops_batch_t b)
+{
+    batch_release(b);
+    return OPS_OK;
+}
+
+// ---------------------------------------------------------------------- autotuner ----
+// Coordinate descent over the row-class thresholds {R8, R16, R32, W, E1, E2}: starting from
+// the handle's current values, each parameter in turn takes each of its candidate values
+// while the others stay fixed, and the fastest value is kept.  A candidate is timed with
+// CUDA events as the median of `reps` complete runs (plan + numeric) of the given batch;
+// pass a representative sample of the real workload.  The best thresholds are installed on
+// the handle and returned.
+namespace {
+
+float time_candidate(ops_handle_s *h, int dtype, int32_t count, const ops_batch_item *items, int reps,
+                     cudaStream_t st, int *status)
+{
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    std::vector<float> ms;
+    *status = OPS_OK;
+    for (int r = 0; r < reps + 1 && *status == OPS_OK; ++r) {
+        cudaEventRecord(e0, st);
+        ops_batch_t b = nullptr;
+        *status = ops_batch_create(h, dtype, count, items, &b, st);
+        if (*status == OPS_OK) *status = ops_batch_execute(b, 0, st);
+        cudaEventRecord(e1, st);
+        cudaEventSynchronize(e1);
+        float t = 0.f;
+        cudaEventElapsedTime(&t, e0, e1);
+        if (r > 0) ms.push_back(t);  // the first run warms the pool and the caches
+        ops_batch_destroy(b);
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (ms.empty()) return 1e30f;
+    std::sort(ms.begin(), ms.end());
+    return ms[ms.size() / 2];
+}
+
+}  // namespace
+
+extern "C" int ops_autotune(ops_handle_t h, int dtype, int32_t count, const ops_batch_item *items, int reps,
+                            int32_t *best, float *best_ms, void *stream)
+{
+    if (!h || !items || count <= 0 || !best || reps < 1) return OPS_INVALID_ARGUMENT;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const Thresholds saved = h->th;
+    int cur[6] = {h->th.r8, h->th.r16, h->th.r32, h->th.w, h->th.e1, h->th.e2};
+    const std::vector<std::vector<int>> cand = {
+        {8, 0}, {16, 0}, {32, 0}, {128, 64, 32, 0}, {1024, 512, 256, 0}, {13312, 4096}};
+    auto apply = [&](const int *v) { h->th = Thresholds{v[0], v[1], v[2], v[3], v[4], v[5]}; };
+    int status = OPS_OK;
+    apply(cur);
+    float best_t = time_candidate(h, dtype, count, items, reps, st, &status);
+    if (status != OPS_OK) {
+        h->th = saved;
+        return status;
+    }
+    for (int p = 0; p < 6; ++p) {
+        for (int v : cand[p]) {
+            if (v == cur[p]) continue;
+            int trial[6];
+            std::memcpy(trial, cur, sizeof(trial));
+            trial[p] = v;
+            apply(trial);
+            const float t = time_candidate(h, dtype, count, items, reps, st, &status);
+            if (status != OPS_OK) {
+                h->th = saved;
+                return status;
+            }
+            if (t < best_t) {
+                best_t = t;
+                std::memcpy(cur, trial, sizeof(cur));
+            }
+        }
+    }
+    apply(cur);
+    std::memcpy(best, cur, sizeof(cur));
+    if (best_ms) *best_ms = best_t;
+    return OPS_OK;
+}
+
+// Tuning records: a JSON object {"<key>": [r8, r16, r32, w, e1, e2], ...} in one file.
+namespace {
+
+std::string read_file(const char *path)
+{
+    FILE *f = std::fopen(path, "rb");
+    if (!f) return std::string();
+    std::string s;
+    char buf[4096];
+    size_t n;
+    while ((n = std::fread(buf, 1, sizeof(buf), f)) > 0) s.append(buf, n);
+    std::fclose(f);
+    return s;
+}
+
+// Parses the records written by ops_tuning_store (keys without quotes or backslashes).
+std::vector<std::pair<std::string, std::vector<int>>> parse_records(const std::string &s)
+{
+    std::vector<std::pair<std::string, std::vector<int>>> out;
+    size_t i = 0;
+    while ((i = s.find('"', i)) != std::string::npos) {
+        const size_t j = s.find('"', i + 1);
+        if (j == std::string::npos) break;
+        std::string key = s.substr(i + 1, j - i - 1);
+        const size_t a = s.find('[', j), b = s.find(']', j);
+        if (a == std::string::npos || b == std::string::npos || b < a) break;
+        std::vector<int> v;
+        const char *p = s.c_str() + a + 1;
+        const char *e = s.c_str() + b;
+        while (p < e) {
+            char *q = nullptr;
+            const long x = std::strtol(p, &q, 10);
+            if (q == p) {
+                ++p;
+                continue;
+            }
+            v.push_back((int)x);
+            p = q;
+        }
+        out.emplace_back(key, v);
+        i = b + 1;
+    }
+    return out;
+}
+
+}  // namespace
+
+extern "C" int ops_tuning_store(const char *path, const char *key, const int32_t *th)
+{
+    if (!path || !key || !th) return OPS_INVALID_ARGUMENT;
+    for (const char *c = key; *c; ++c)
+        if (*c == '"' || *c == '\\') return OPS_INVALID_ARGUMENT;
+    auto recs = parse_records(read_file(path));
+    std::vector<int> v(th, th + 6);
+    bool found = false;
+    for (auto &r : recs)
+        if (r.first == key) {
+            r.second = v;
+            found = true;
+        }
+    if (!found) recs.emplace_back(key, v);
+    FILE *f = std::fopen(path, "wb");
+    if (!f) return OPS_EXCEPTION;
+    std::fprintf(f, "{\n");
+    for (size_t k = 0; k < recs.size(); ++k) {
+        std::fprintf(f, "  \"%s\": [", recs[k].first.c_str());
+        for (size_t t = 0; t < recs[k].second.size(); ++t) std::fprintf(f, t ? ", %d" : "%d", recs[k].second[t]);
+        std::fprintf(f, "]%s\n", k + 1 < recs.size() ? "," : "");
+    }
+    std::fprintf(f, "}\n");
+    std::fclose(f);
+    return OPS_OK;
+}
+
+extern "C" int ops_tuning_lookup(const char *path, const char *key, int32_t *th)
+{
+    if (!path || !key || !th) return OPS_INVALID_ARGUMENT;
+    for (const auto &r : parse_records(read_file(path)))
+        if (r.first == key && r.second.size() == 6) {
+            std::memcpy(th, r.second.data(), 6 * sizeof(int32_t));
+            return OPS_OK;
+        }
+    return OPS_NOT_SUPPORTED;
+}

@@ -34,6 +34,19 @@ constexpr int kEsc1AMax = 1024;
 constexpr int kEsc2FlopMax = 13312;
 constexpr int kEsc2AMax = 2560;
 
+// Runtime row-class thresholds (the autotuner's search space).  Each bound is capped by
+// the compiled capacity of its kernel; a bound of 0 switches the class off.
+struct Thresholds {
+    int r8;   // <= kSmallFlopMax
+    int r16;  // <= 16
+    int r32;  // <= 32
+    int w;    // <= kWarpFlopMax
+    int e1;   // <= kEsc1FlopMax
+    int e2;   // <= kEsc2FlopMax
+};
+
+__host__ __device__ inline Thresholds default_thresholds() { return Thresholds{8, 16, 32, 128, 1024, 13312}; }
+
 // Error bits written by kernels into DevInfo::flags (read back by the host).
 enum : int {
     kErrRowFlopOverflow = 1,  // a row has more than INT_MAX intermediate products
@@ -50,6 +63,7 @@ struct DevInfo {
     unsigned long long total_flop;
     unsigned long long total_nnz;
     int next[2][kNumClasses];     // dynamic row cursors of the [symbolic, numeric] kernels
+    int split[2];                 // E1 rows re-binned for the numeric phase: [hash, expand/sort]
 };
 
 __device__ __forceinline__ int lane_id() { return threadIdx.x & 31; }

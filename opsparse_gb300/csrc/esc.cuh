@@ -136,7 +136,7 @@ __device__ __forceinline__ int esc_scan_row(const SpgemmArgs<T> &g, int a0, int 
 
 template <typename Shape, bool kNum, typename T>
 __global__ void __launch_bounds__(Shape::kThreads) k_esc_rows(SpgemmArgs<T> g, const int *__restrict__ list,
-                                                              int count, int *cursor)
+                                                              const int *count_ptr, int *cursor)
 {
     using AccT = Acc<T>;
     using S = typename AccT::S;
@@ -179,6 +179,7 @@ __global__ void __launch_bounds__(Shape::kThreads) k_esc_rows(SpgemmArgs<T> g, c
         p += sizeof(unsigned short) * PCAP;
         own = reinterpret_cast<unsigned short *>(p);
     }
+    const int count = *count_ptr;
     const int key_bits = max(1, ceil_log2(max(g.N, 2)));
     const int passes = (key_bits + 7) / 8;
 
@@ -344,6 +345,39 @@ __global__ void __launch_bounds__(Shape::kThreads) k_esc_rows(SpgemmArgs<T> g, c
         }
     }
     if constexpr (!kNum) block_add_u64(nnz_acc, &g.info->total_nnz);
+}
+
+// Numeric re-binning of the E1 rows by their output size (known after the symbolic
+// phase): rows with at most kSplitNnz outputs go to the warp-hash numeric kernel (few
+// outputs per product: hashing beats sorting every product), the rest stay with
+// expand/sort/compress.  Counts go to out_counts[0..1] on the device.
+constexpr int kSplitNnz = 256;
+
+static __global__ void k_split_by_nnz(const int *__restrict__ list, const int *count_ptr, const int *__restrict__ c_rpt,
+                                      int *hash_list, int *esc_list, int *out_counts)
+{
+    const int count = *count_ptr;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i - (int)threadIdx.x < count; i += gridDim.x * blockDim.x) {
+        const bool in = i < count;
+        int r = 0;
+        bool small = false;
+        if (in) {
+            r = list[i];
+            small = c_rpt[r + 1] - c_rpt[r] <= kSplitNnz;
+        }
+        const unsigned ms = __ballot_sync(kFull, in && small);
+        const unsigned ml = __ballot_sync(kFull, in && !small);
+        const int lane = lane_id();
+        int bs = 0, bl = 0;
+        if (lane == 0) {
+            if (ms) bs = atomicAdd(&out_counts[0], __popc(ms));
+            if (ml) bl = atomicAdd(&out_counts[1], __popc(ml));
+        }
+        bs = __shfl_sync(kFull, bs, 0);
+        bl = __shfl_sync(kFull, bl, 0);
+        if (in && small) hash_list[bs + __popc(ms & lanemask_lt())] = r;
+        if (in && !small) esc_list[bl + __popc(ml & lanemask_lt())] = r;
+    }
 }
 
 // Orders a class list by product count, largest first, so that with dynamic row

@@ -71,6 +71,8 @@ struct ops_handle_s {
     long long plan_nnz = 0;
 
     size_t map_budget = size_t(8) << 30;  // largest product map the backward may keep
+    opsg::Thresholds th = opsg::default_thresholds();
+    opsg::Thresholds plan_th = opsg::default_thresholds();  // thresholds the current plan was built with
     BackwardPlan bwd;
 
     std::string last_error;

@@ -82,7 +82,7 @@ static __global__ void __launch_bounds__(kSetupThreads) k_setup(const int *__res
                                                         const int *__restrict__ brpt, const int *__restrict__ bcol,
                                                         int M, int K, int N, int *__restrict__ row_flop,
                                                         int *__restrict__ lists, int *__restrict__ c_rownnz,
-                                                        DevInfo *info)
+                                                        DevInfo *info, Thresholds th)
 {
     __shared__ int s_keys[kSmallFlopMax][kSetupThreads];  // R8 rows: the row's column keys
     __shared__ int s_cnt[kNumClasses];
@@ -143,7 +143,7 @@ static __global__ void __launch_bounds__(kSetupThreads) k_setup(const int *__res
         row_flop[r] = f32;
         if (flop == 0) {
             c_rownnz[r] = 0;
-        } else if (!bad && flop <= kSmallFlopMax && lenA <= kSmallFlopMax) {
+        } else if (!bad && flop <= th.r8 && lenA <= th.r8) {
             // R8 row: its symbolic phase happens here — gather the <= 8 column keys and
             // count the distinct ones.  These rows join no list; the numeric phase walks
             // them in row order (k_small_rows).
@@ -162,15 +162,15 @@ static __global__ void __launch_bounds__(kSetupThreads) k_setup(const int *__res
                 small_nnz += dup ? 0u : 1u;
             }
             c_rownnz[r] = (int)small_nnz;
-        } else if (flop <= 16 && lenA <= 16) {
+        } else if (flop <= th.r16 && lenA <= 16) {
             cls = kClsR16;
-        } else if (flop <= 32 && lenA <= 32) {
+        } else if (flop <= th.r32 && lenA <= 32) {
             cls = kClsR32;
-        } else if (flop <= kWarpFlopMax) {
+        } else if (flop <= th.w) {
             cls = kClsW;
-        } else if (flop <= kEsc1FlopMax && lenA <= kEsc1AMax) {
+        } else if (flop <= th.e1 && lenA <= kEsc1AMax) {
             cls = kClsE1;
-        } else if (flop <= kEsc2FlopMax && lenA <= kEsc2AMax) {
+        } else if (flop <= th.e2 && lenA <= kEsc2AMax) {
             cls = kClsE2;
         } else {
             cls = kClsD;
@@ -226,7 +226,7 @@ static __global__ void __launch_bounds__(kSetupThreads) k_setup(const int *__res
 constexpr int kSmallThreads = 256;
 
 template <typename T>
-__global__ void __launch_bounds__(kSmallThreads) k_small_rows(SpgemmArgs<T> g)
+__global__ void __launch_bounds__(kSmallThreads) k_small_rows(SpgemmArgs<T> g, int r8)
 {
     using AccT = Acc<T>;
     __shared__ int s_key[kSmallFlopMax][kSmallThreads];
@@ -237,7 +237,7 @@ __global__ void __launch_bounds__(kSmallThreads) k_small_rows(SpgemmArgs<T> g)
         const int flop = __ldg(g.row_flop + r);
         const int a0 = __ldg(g.arpt + r);
         const int a1 = __ldg(g.arpt + r + 1);
-        if (flop == 0 || flop > kSmallFlopMax || a1 - a0 > kSmallFlopMax) continue;
+        if (flop == 0 || flop > r8 || a1 - a0 > r8) continue;
         int n = 0;
         for (int p = a0; p < a1; ++p) {
             const int j = __ldg(g.acol + p);
@@ -372,8 +372,10 @@ __global__ void __launch_bounds__(256) k_reg_rows(SpgemmArgs<T> g, const int *__
 }
 
 // ==================================================================================
-// W class: one warp per row, open-addressing table of nextpow2(2*n) <= kWarpTableMax
-// slots in shared memory (n = flop in symbolic, nnz in numeric).  Products are visited
+// Warp-per-row hash kernel (W class, and E1 rows whose outputs are few): one warp per
+// row, open-addressing table of nextpow2(2*n) <= TMAX slots in shared memory (n = flop in
+// symbolic, nnz in numeric).  The row count is read from device memory (count_ptr) so
+// lists split on the device need no host round trip.  Products are visited
 // in j-major chunks of 32 by warp_products; within a chunk, match groups are folded by
 // their leader, and chunks are separated by __syncwarp, so each slot sees its
 // contributions in ascending j.  Numeric then compacts the table and places each entry
@@ -381,9 +383,15 @@ __global__ void __launch_bounds__(256) k_reg_rows(SpgemmArgs<T> g, const int *__
 // ==================================================================================
 constexpr int kWarpRowsThreads = 256;
 
-template <bool kNum, typename T>
+template <bool kNum, typename T, int TMAX>
+constexpr size_t warp_rows_smem()
+{
+    return (size_t)(kWarpRowsThreads / 32) * TMAX * (sizeof(int) + (kNum ? sizeof(typename Acc<T>::S) : 0));
+}
+
+template <bool kNum, typename T, int TMAX>
 __global__ void __launch_bounds__(kWarpRowsThreads) k_warp_rows(SpgemmArgs<T> g, const int *__restrict__ list,
-                                                                int count)
+                                                                const int *count_ptr)
 {
     using AccT = Acc<T>;
     using S = typename AccT::S;
@@ -391,9 +399,9 @@ __global__ void __launch_bounds__(kWarpRowsThreads) k_warp_rows(SpgemmArgs<T> g,
     const int lane = lane_id();
     const int warp = threadIdx.x >> 5;
     constexpr int kWarps = kWarpRowsThreads / 32;
-    S *vals = reinterpret_cast<S *>(smem_raw) + warp * kWarpTableMax;
-    int *keys = reinterpret_cast<int *>(smem_raw + (kNum ? sizeof(S) * kWarps * kWarpTableMax : 0)) +
-                warp * kWarpTableMax;
+    const int count = *count_ptr;
+    S *vals = reinterpret_cast<S *>(smem_raw) + warp * TMAX;
+    int *keys = reinterpret_cast<int *>(smem_raw + (kNum ? sizeof(S) * kWarps * TMAX : 0)) + warp * TMAX;
     const long long warp0 = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
     unsigned long long nnz_acc = 0;

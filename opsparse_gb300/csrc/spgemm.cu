@@ -42,8 +42,12 @@ struct Mat {
 template <typename T>
 void set_smem_attrs()
 {
-    cudaFuncSetAttribute(k_warp_rows<true, T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)(sizeof(typename Acc<T>::S) + sizeof(int)) * kWarpTableMax * (kWarpRowsThreads / 32));
+    cudaFuncSetAttribute(k_warp_rows<true, T, kWarpTableMax>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)warp_rows_smem<true, T, kWarpTableMax>());
+    cudaFuncSetAttribute(k_warp_rows<false, T, 2 * kEsc1FlopMax>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)warp_rows_smem<false, T, 2 * kEsc1FlopMax>());
+    cudaFuncSetAttribute(k_warp_rows<true, T, 2 * kSplitNnz>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)warp_rows_smem<true, T, 2 * kSplitNnz>());
     cudaFuncSetAttribute(k_esc_rows<EscSmall, true, T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)EscSmall::kNumericSmem);
     cudaFuncSetAttribute(k_esc_rows<EscLarge, true, T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -59,7 +63,8 @@ int ensure_ws(ops_handle_s *h, int M, cudaStream_t st)
     if (h->ws && h->ws_M >= M) return OPS_OK;
     size_t cub_bytes = 0;
     OPS_CUDA(h, cub::DeviceScan::ExclusiveSum(nullptr, cub_bytes, (int *)nullptr, (int *)nullptr, M + 1, st));
-    const size_t lists_b = align_up(sizeof(int) * (size_t)kNumClasses * (size_t)M, 256);
+    // one list per class plus two for the numeric re-binning of E1 rows
+    const size_t lists_b = align_up(sizeof(int) * (size_t)(kNumClasses + 2) * (size_t)M, 256);
     const size_t flop_b = align_up(sizeof(int) * (size_t)M, 256);
     const size_t info_b = align_up(sizeof(DevInfo), 256);
     const size_t total = lists_b + flop_b + info_b + align_up(cub_bytes, 256);
@@ -146,7 +151,7 @@ int launch_classes(ops_handle_s *h, const SpgemmArgs<T> &g, cudaStream_t st)
         if (h->timing >= 2) OPS_CUDA(h, cudaEventRecord(h->ev_k[kNum][c][0], s));
         switch (c) {
             case kClsR8:  // numeric only: walks the rows in order
-                k_small_rows<T><<<grid_for(g.M, kSmallThreads, sms * 8), kSmallThreads, 0, s>>>(g);
+                k_small_rows<T><<<grid_for(g.M, kSmallThreads, sms * 8), kSmallThreads, 0, s>>>(g, h->plan_th.r8);
                 break;
             case kClsR16:
                 k_reg_rows<16, kNum, T><<<grid_for((n + 1) / 2, 8, sms * 8), 256, 0, s>>>(g, list, n);
@@ -155,22 +160,38 @@ int launch_classes(ops_handle_s *h, const SpgemmArgs<T> &g, cudaStream_t st)
                 k_reg_rows<32, kNum, T><<<grid_for(n, 8, sms * 8), 256, 0, s>>>(g, list, n);
                 break;
             case kClsW: {
-                const size_t smem = (kNum ? sizeof(typename Acc<T>::S) + sizeof(int) : sizeof(int)) *
-                                    (size_t)kWarpTableMax * (kWarpRowsThreads / 32);
-                k_warp_rows<kNum, T><<<grid_for(n, kWarpRowsThreads / 32, sms * 8), kWarpRowsThreads, smem, s>>>(
-                    g, list, n);
+                k_warp_rows<kNum, T, kWarpTableMax>
+                    <<<grid_for(n, kWarpRowsThreads / 32, sms * 8), kWarpRowsThreads,
+                       warp_rows_smem<kNum, T, kWarpTableMax>(), s>>>(g, list, &h->info->counts[c]);
                 break;
             }
             case kClsE1: {
-                const size_t smem = kNum ? EscSmall::kNumericSmem : EscSmall::kSymbolicSmem;
-                k_esc_rows<EscSmall, kNum, T><<<std::min(n, sms * 8), EscSmall::kThreads, smem, s>>>(
-                    g, list, n, &h->info->next[kNum][c]);
+                if (!kNum) {  // distinct-column count: one warp per row, table of 2*flop slots
+                    k_warp_rows<false, T, 2 * kEsc1FlopMax>
+                        <<<grid_for(n, kWarpRowsThreads / 32, sms * 3), kWarpRowsThreads,
+                           warp_rows_smem<false, T, 2 * kEsc1FlopMax>(), s>>>(g, list, &h->info->counts[c]);
+                } else {  // re-bin by output size, then hash (few outputs) or expand/sort/compress
+                    int *hash_list = h->lists + (size_t)kNumClasses * (size_t)h->plan_M;
+                    int *esc_list = hash_list + h->plan_M;
+                    k_split_by_nnz<<<grid_for(n, 256, sms * 4), 256, 0, s>>>(list, &h->info->counts[c], g.c_rpt,
+                                                                           hash_list, esc_list, h->info->split);
+                    OPS_CUDA(h, cudaGetLastError());
+                    ++h->launches;
+                    k_warp_rows<true, T, 2 * kSplitNnz>
+                        <<<grid_for(n, kWarpRowsThreads / 32, sms * 4), kWarpRowsThreads,
+                           warp_rows_smem<true, T, 2 * kSplitNnz>(), s>>>(g, hash_list, &h->info->split[0]);
+                    OPS_CUDA(h, cudaGetLastError());
+                    ++h->launches;
+                    k_esc_rows<EscSmall, true, T><<<std::min(n, sms * 8), EscSmall::kThreads,
+                                                   EscSmall::kNumericSmem, s>>>(g, esc_list, &h->info->split[1],
+                                                                                &h->info->next[1][c]);
+                }
                 break;
             }
             case kClsE2: {
                 const size_t smem = kNum ? EscLarge::kNumericSmem : EscLarge::kSymbolicSmem;
                 k_esc_rows<EscLarge, kNum, T><<<std::min(n, sms), EscLarge::kThreads, smem, s>>>(
-                    g, list, n, &h->info->next[kNum][c]);
+                    g, list, &h->info->counts[c], &h->info->next[kNum][c]);
                 break;
             }
             case kClsD: {
@@ -223,7 +244,7 @@ int run_symbolic(ops_handle_s *h, const Mat &A, const Mat &B, int *c_rpt, long l
     if (h->timing) OPS_CUDA(h, cudaEventRecord(h->ev_t[1], st));
     if (M > 0) {
         k_setup<<<(M + kSetupThreads - 1) / kSetupThreads, kSetupThreads, 0, st>>>(
-            A.rpt, A.col, B.rpt, B.col, M, A.cols, B.cols, h->row_flop, h->lists, c_rpt, h->info);
+            A.rpt, A.col, B.rpt, B.col, M, A.cols, B.cols, h->row_flop, h->lists, c_rpt, h->info, h->th);
         OPS_CUDA(h, cudaGetLastError());
         ++h->launches;
     }
@@ -235,6 +256,7 @@ int run_symbolic(ops_handle_s *h, const Mat &A, const Mat &B, int *c_rpt, long l
     if (hi.flags & kErrRowFlopOverflow)
         return fail(h, OPS_INT32_OVERFLOW, "a row of C has more than INT32_MAX intermediate products");
     std::memcpy(h->counts, hi.counts, sizeof(h->counts));
+    h->plan_th = h->th;
     h->plan_M = M;
     h->plan_K = A.cols;
     h->plan_N = B.cols;
@@ -282,6 +304,7 @@ int run_numeric(ops_handle_s *h, const Mat &A, const Mat &B, const int *c_rpt, i
     if (h->counts[kClsD] > 0) OPS_CHECK(ensure_dense(h, B.cols, h->counts[kClsD], st));
     OPS_CUDA(h, cudaMemsetAsync(&h->info->flags, 0, sizeof(int), st));
     OPS_CUDA(h, cudaMemsetAsync(h->info->next[1], 0, sizeof(h->info->next[1]), st));
+    OPS_CUDA(h, cudaMemsetAsync(h->info->split, 0, sizeof(h->info->split), st));
     SpgemmArgs<T> g{};
     g.arpt = A.rpt;
     g.acol = A.col;
@@ -467,6 +490,28 @@ int ops_handle_set_dense_budget(ops_handle_t h, size_t bytes)
 {
     if (!h) return OPS_INVALID_ARGUMENT;
     h->dense_budget = bytes;
+    return OPS_OK;
+}
+
+int ops_handle_set_thresholds(ops_handle_t h, const int32_t *th, int n)
+{
+    if (!h || !th || n != 6) return OPS_INVALID_ARGUMENT;
+    const Thresholds cap = default_thresholds();
+    Thresholds t{th[0], th[1], th[2], th[3], th[4], th[5]};
+    if (t.r8 < 0 || t.r8 > cap.r8 || t.r16 < 0 || t.r16 > cap.r16 || t.r32 < 0 || t.r32 > cap.r32 || t.w < 0 ||
+        t.w > cap.w || t.e1 < 0 || t.e1 > cap.e1 || t.e2 < 0 || t.e2 > cap.e2)
+        return fail(h, OPS_INVALID_ARGUMENT, "threshold above the compiled capacity of its class");
+    h->th = t;
+    h->plan_valid = false;
+    return OPS_OK;
+}
+
+int ops_handle_get_thresholds(ops_handle_t h, int32_t *th, int n)
+{
+    if (!h || !th || n != 6) return OPS_INVALID_ARGUMENT;
+    const Thresholds t = h->th;
+    const int32_t v[6] = {t.r8, t.r16, t.r32, t.w, t.e1, t.e2};
+    std::memcpy(th, v, sizeof(v));
     return OPS_OK;
 }
 
