@@ -52,6 +52,13 @@ def make_workload(name: str):
         rpt, col, val = gen.laplacian2d(128)
         desc = {"workload": "laplacian2d_128x128", "rows": 16384, "op": "C=A*A"}
         dt = "f64"
+    elif name == "powerlaw_AAt":
+        a = gen.powerlaw_square(200_000, 16, 2.2)
+        b = gen.transpose_pattern(a[0], a[1], 200_000)
+        desc = {"workload": "powerlaw_200k_AAt", "rows": 200_000, "mean_degree": 16, "exponent": 2.2,
+                "values": "N(0,1)", "op": "C=A*B, B = pattern(A^T) with fresh values", "seed": gen.SEED}
+        n = 200_000
+        return desc, "f64", (a, b), n
     elif name in ("stencil27", "stencil27_f32"):
         rpt, col, val = gen.stencil27(80)
         desc = {"workload": "stencil27_80^3", "rows": 512000, "values": "N(0,1)", "op": "C=A*A", "seed": gen.SEED}
@@ -321,7 +328,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="web",
-                    choices=["web", "laplacian", "stencil27", "stencil27_f32", "batched", "backward", "backward_f32"])
+                    choices=["web", "laplacian", "stencil27", "stencil27_f32", "powerlaw_AAt", "batched", "backward",
+                             "backward_f32"])
     ap.add_argument("--batch", type=int, default=4096, help="problems in the batched workload")
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
     args = ap.parse_args()

@@ -196,6 +196,37 @@ __device__ __forceinline__ void warp_products(int a_begin, int a_end, int stride
     }
 }
 
+// Row-aligned enumeration for rows whose B rows are long: the warp loads 32 A entries at
+// a time, then walks them in order with the lanes spread over one B row per step
+// (several steps for B rows longer than 32).  A B row's columns are distinct, so the
+// lanes of a step never share a key: no de-duplication is needed, and successive steps
+// (ascending j) are separated by the caller's __syncwarp.  f(valid, k, a) is called once
+// per step with all lanes converged.
+template <bool kNeedVal, typename T, typename F>
+__device__ __forceinline__ void warp_rowwise_products(int a_begin, int a_end, const int *__restrict__ acol,
+                                                      const T *__restrict__ aval, const int *__restrict__ brpt, F &&f)
+{
+    const int lane = lane_id();
+    for (int wa = a_begin; wa < a_end; wa += 32) {
+        const int q = wa + lane;
+        int b0 = 0, b1 = 0;
+        T av = T(0);
+        if (q < a_end) {
+            const int j = __ldg(acol + q);
+            b0 = __ldg(brpt + j);
+            b1 = __ldg(brpt + j + 1);
+            if (kNeedVal) av = __ldg(aval + q);
+        }
+        const int m = min(32, a_end - wa);
+        for (int t = 0; t < m; ++t) {
+            const int s0 = __shfl_sync(kFull, b0, t);
+            const int s1 = __shfl_sync(kFull, b1, t);
+            const T a = kNeedVal ? shfl(av, t) : T(0);
+            for (int c = s0; c < s1; c += 32) f(c + lane < s1, c + lane, a);
+        }
+    }
+}
+
 // Claim (or find) the slot of `key` in an open-addressing table of ts = 2^log_ts
 // slots.  Linear probing, bounded by the table size; returns -1 (and raises
 // kErrProbeLimit) only if the table is full, which the sizing rules exclude.

@@ -425,6 +425,22 @@ __global__ void __launch_bounds__(kWarpRowsThreads) k_warp_rows(SpgemmArgs<T> g,
         }
         __syncwarp();
         int cnt = 0;
+        const int row_products = kNum ? __ldg(g.row_flop + r) : n_expect;
+        if (row_products >= 16 * (a1 - a0)) {
+            // long B rows: one B row per step, every lane owns a distinct key
+            warp_rowwise_products<kNum, T>(a0, a1, g.acol, g.aval, g.brpt, [&](bool valid, int k, T av) {
+                if (valid) {
+                    const int col = __ldg(g.bcol + k);
+                    bool is_new = false;
+                    const int slot = table_claim(keys, col, log_ts, &is_new, &g.info->flags);
+                    cnt += is_new ? 1 : 0;
+                    if constexpr (kNum) {
+                        if (slot >= 0) vals[slot] = AccT::step(vals[slot], av, __ldg(g.bval + k));
+                    }
+                }
+                __syncwarp();
+            });
+        } else
         warp_products<kNum, T>(a0, a1, 32, g.acol, g.aval, g.brpt, [&](bool valid, int k, T av, int) {
             const int col = valid ? __ldg(g.bcol + k) : kEmpty;
             const unsigned m = __match_any_sync(kFull, col);
@@ -468,12 +484,41 @@ __global__ void __launch_bounds__(kWarpRowsThreads) k_warp_rows(SpgemmArgs<T> g,
             }
             if (n != n_expect && lane == 0) atomicOr(&g.info->flags, kErrCountMismatch);
             const int nw = min(n, n_expect);
-            for (int e = lane; e < nw; e += 32) {
-                const int ke = keys[e];
-                int rank = 0;
-                for (int t = 0; t < nw; ++t) rank += keys[t] < ke ? 1 : 0;
-                g.c_col[off + rank] = ke;
-                g.c_val[off + rank] = AccT::fin(vals[e]);
+            if (nw <= 32) {  // rank among at most 32 keys
+                for (int e = lane; e < nw; e += 32) {
+                    const int ke = keys[e];
+                    int rank = 0;
+                    for (int t = 0; t < nw; ++t) rank += keys[t] < ke ? 1 : 0;
+                    g.c_col[off + rank] = ke;
+                    g.c_val[off + rank] = AccT::fin(vals[e]);
+                }
+            } else {  // bitonic sort of the compacted entries, padded with INT_MAX keys
+                int m = 64;
+                while (m < nw) m <<= 1;  // m <= ts: the table holds at least 2*n slots
+                for (int i = nw + lane; i < m; i += 32) keys[i] = INT_MAX;
+                __syncwarp();
+                for (int k2 = 2; k2 <= m; k2 <<= 1) {
+                    for (int j2 = k2 >> 1; j2 > 0; j2 >>= 1) {
+                        for (int i = lane; i < m; i += 32) {
+                            const int ixj = i ^ j2;
+                            if (ixj > i) {
+                                const int ki = keys[i], kx = keys[ixj];
+                                if ((ki > kx) == ((i & k2) == 0)) {
+                                    keys[i] = kx;
+                                    keys[ixj] = ki;
+                                    const S tv = vals[i];
+                                    vals[i] = vals[ixj];
+                                    vals[ixj] = tv;
+                                }
+                            }
+                        }
+                        __syncwarp();
+                    }
+                }
+                for (int e = lane; e < nw; e += 32) {
+                    g.c_col[off + e] = keys[e];
+                    g.c_val[off + e] = AccT::fin(vals[e]);
+                }
             }
             __syncwarp();
         }
