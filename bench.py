@@ -138,16 +138,21 @@ class ClockSampler:
 
 
 # ----------------------------------------------------------------------------- CPU side
+def _pair(data):
+    """Plain workloads are C = A*A (one CSR triple) or C = A*B (a pair of triples)."""
+    return (data, data) if len(data) == 3 else data
+
+
 def cpu_baseline(data, n, steps=3):
     import oracle
 
-    rpt, col, val = data
-    val64 = np.asarray(val, dtype=np.float64)
-    oracle.omp_spgemm(rpt, col, val64, rpt, col, val64)  # warm-up
+    (ar, ac, av), (br, bc, bv) = _pair(data)
+    av64, bv64 = np.asarray(av, dtype=np.float64), np.asarray(bv, dtype=np.float64)
+    oracle.omp_spgemm(ar, ac, av64, br, bc, bv64)  # warm-up
     ts = []
     for _ in range(steps):
         t0 = time.perf_counter()
-        oracle.omp_spgemm(rpt, col, val64, rpt, col, val64)
+        oracle.omp_spgemm(ar, ac, av64, br, bc, bv64)
         ts.append(time.perf_counter() - t0)
     return statistics.median(ts), oracle.num_threads()
 
@@ -157,15 +162,15 @@ def run_reference(args, desc, dt, data, n, rank, world):
         return
     import oracle
 
-    P = int(oracle.flop(data[0], data[1], data[0])[0])
-    rpt, col, val = data
-    val64 = np.asarray(val, dtype=np.float64)
+    (ar, ac, av), (br, bc, bv) = _pair(data)
+    P = int(oracle.flop(ar, ac, br)[0])
+    av64, bv64 = np.asarray(av, dtype=np.float64), np.asarray(bv, dtype=np.float64)
     for _ in range(max(0, args.warmup)):
-        oracle.omp_spgemm(rpt, col, val64, rpt, col, val64)
+        oracle.omp_spgemm(ar, ac, av64, br, bc, bv64)
     ts = []
     for _ in range(args.steps):
         t0 = time.perf_counter()
-        oracle.omp_spgemm(rpt, col, val64, rpt, col, val64)
+        oracle.omp_spgemm(ar, ac, av64, br, bc, bv64)
         ts.append(time.perf_counter() - t0)
     t = statistics.mean(ts)
     gf = 2.0 * P / t / 1e9
@@ -191,20 +196,22 @@ def run_ours(args, desc, dt, data, n, rank, world, local_rank):
     dev = torch.device("cuda", local_rank)
     tdt = torch.float64 if dt == "f64" else torch.float32
     s = 8 if dt == "f64" else 4
-    rpt, col, val = data
+    (rpt, col, val), (brpt, bcol, bval) = _pair(data)
+    same = len(data) == 3
     A = ops.csr_to_device(rpt, col, val, n, n, dtype=tdt, device=str(dev))
+    B = A if same else ops.csr_to_device(brpt, bcol, bval, n, n, dtype=tdt, device=str(dev))
     lib = capi.load()
     h = ops.Handle()
     stream = torch.cuda.current_stream()
     st = C.c_void_p(stream.cuda_stream)
     code = capi.OPS_F64 if dt == "f64" else capi.OPS_F32
     flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device=dev)
-    ap = A.ptrs()
+    ap, bp = A.ptrs(), B.ptrs()
 
     def step():
         rp, cp, vp = C.c_void_p(), C.c_void_p(), C.c_void_p()
         nnz = C.c_int64(0)
-        capi.check(lib.ops_spgemm(h.h, code, n, n, n, ap[0], ap[1], ap[2], A.nnz, ap[0], ap[1], ap[2], A.nnz,
+        capi.check(lib.ops_spgemm(h.h, code, n, n, n, ap[0], ap[1], ap[2], A.nnz, bp[0], bp[1], bp[2], B.nnz,
                                   C.byref(rp), C.byref(cp), C.byref(vp), C.byref(nnz), st), h.h)
         return rp, cp, vp, int(nnz.value)
 
@@ -249,8 +256,10 @@ def run_ours(args, desc, dt, data, n, rank, world, local_rank):
     gflops = world * 2.0 * P / (t_ms * 1e-3) / 1e9
 
     # end to end through the same call with host buffers
-    pin = [torch.as_tensor(x).pin_memory() for x in (rpt, col, val)]
+    host_in = (rpt, col, val) if same else (rpt, col, val, brpt, bcol, bval)
+    pin = [torch.as_tensor(x).pin_memory() for x in host_in]
     d_in = [torch.empty_like(x, device=dev) for x in pin]
+    d_b = d_in[:3] if same else d_in[3:]
     h_out = [torch.empty(n + 1, dtype=torch.int32).pin_memory(), torch.empty(max(nnz_c, 1), dtype=torch.int32).pin_memory(),
              torch.empty(max(nnz_c, 1), dtype=tdt).pin_memory()]
     h2d = sum(x.numel() * x.element_size() for x in pin)
@@ -265,7 +274,7 @@ def run_ours(args, desc, dt, data, n, rank, world, local_rank):
         rp2, cp2, vp2 = C.c_void_p(), C.c_void_p(), C.c_void_p()
         nnz = C.c_int64(0)
         capi.check(lib.ops_spgemm(h.h, code, n, n, n, d_in[0].data_ptr(), d_in[1].data_ptr(), d_in[2].data_ptr(),
-                                  A.nnz, d_in[0].data_ptr(), d_in[1].data_ptr(), d_in[2].data_ptr(), A.nnz,
+                                  A.nnz, d_b[0].data_ptr(), d_b[1].data_ptr(), d_b[2].data_ptr(), B.nnz,
                                   C.byref(rp2), C.byref(cp2), C.byref(vp2), C.byref(nnz), st), h.h)
         vstr = "<f8" if dt == "f64" else "<f4"
         for hb, dp, cnt, ts in ((h_out[0], rp2, n + 1, "<i4"), (h_out[1], cp2, nnz_c, "<i4"),
@@ -288,7 +297,7 @@ def run_ours(args, desc, dt, data, n, rank, world, local_rank):
         return
     peak, peak_kind = measured_peak()
     nnz_a = len(col)
-    balg = bytes_alg(n, n, nnz_a, nnz_a, nnz_c, s)
+    balg = bytes_alg(n, n, nnz_a, len(bcol), nnz_c, s)
     achieved = balg / (t_ms * 1e-3) / 1e9
     kms = phases["kernel_ms"]
     names = ["R8", "R16", "R32", "W", "E1", "E2", "D"]

@@ -93,6 +93,11 @@ int ops_handle_set_thresholds(ops_handle_t handle, const int32_t *thresholds, in
 int ops_handle_get_thresholds(ops_handle_t handle, int32_t *thresholds, int count);
 /* Message for the last failing call on this handle ("" if none). */
 const char *ops_handle_last_error(ops_handle_t handle);
+/* Rows handled by each sub-kernel in the last call (synchronises the handle's device
+ * counters to the host): out[0..2] = E1 numeric rows by warp sort, warp hash and
+ * expand/sort/compress; out[3..4] = E2 rows by the mid and the large expand/sort/compress
+ * shape.  Diagnostic; no OpSparse counterpart. */
+int ops_handle_subclass_rows(ops_handle_t handle, int32_t *out, int count);
 const char *ops_status_string(int status);
 
 /* ------------------------------------------------------------------- spgemm -- */

@@ -124,6 +124,13 @@ class Handle:
         check(self.lib.ops_handle_get_timings(self.h, C.byref(t)), self.h)
         return t.as_dict()
 
+    def subclass_rows(self) -> dict:
+        """Rows per sub-kernel of the last call: E1 numeric (warp sort, warp hash,
+        expand/sort/compress) and E2 (mid, large shape)."""
+        arr = (C.c_int32 * 5)()
+        check(self.lib.ops_handle_subclass_rows(self.h, arr, 5), self.h)
+        return dict(zip(("e1_sort", "e1_hash", "e1_esc", "e2_mid", "e2_large"), list(arr)))
+
     # -- two-phase ------------------------------------------------------------
     def symbolic(self, A: CsrMatrix, B: CsrMatrix, c_rpt=None, stream=None):
         torch = _torch()

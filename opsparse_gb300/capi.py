@@ -77,6 +77,7 @@ _SIGS = {
     "ops_handle_set_thresholds": (C.c_int, [P, C.POINTER(I32), C.c_int]),
     "ops_handle_get_thresholds": (C.c_int, [P, C.POINTER(I32), C.c_int]),
     "ops_handle_last_error": (C.c_char_p, [P]),
+    "ops_handle_subclass_rows": (C.c_int, [P, C.POINTER(I32), C.c_int]),
     "ops_spgemm": (C.c_int, [P, C.c_int, I32, I32, I32, P, P, P, I64, P, P, P, I64,
                              C.POINTER(P), C.POINTER(P), C.POINTER(P), C.POINTER(I64), P]),
     "ops_spgemm_symbolic": (C.c_int, [P, I32, I32, I32, P, P, I64, P, P, I64, P, C.POINTER(I64), P]),

@@ -26,6 +26,11 @@ enum RowClass : int {
     kNumClasses = 7
 };
 
+// Extra device lists after the kNumClasses class lists: the numeric re-binning of the E1
+// rows and the size split of the E2 rows.
+enum : int { kXlE1Sort = 0, kXlE1Hash = 1, kXlE1Esc = 2, kXlE2Mid = 3, kXlE2Large = 4, kNumExtraLists = 5 };
+constexpr int kNumLists = kNumClasses + kNumExtraLists;
+
 constexpr int kSmallFlopMax = 8;   // R8 rows: symbolic inside k_setup, numeric k_small_rows
 constexpr int kWarpFlopMax = 128;  // W rows: table of nextpow2(2*flop) <= 256 slots per warp
 constexpr int kWarpTableMax = 256;
@@ -63,7 +68,9 @@ struct DevInfo {
     unsigned long long total_flop;
     unsigned long long total_nnz;
     int next[2][kNumClasses];     // dynamic row cursors of the [symbolic, numeric] kernels
-    int split[2];                 // E1 rows re-binned for the numeric phase: [hash, expand/sort]
+    int split[3];                 // E1 rows re-binned for the numeric phase: [warp sort, hash, expand/sort]
+    int split2[2];                // E2 rows by size, fixed at the symbolic phase: [mid shape, large shape]
+    int next_mid[2];              // row cursor of the mid-shape E2 kernel [symbolic, numeric]
 };
 
 __device__ __forceinline__ int lane_id() { return threadIdx.x & 31; }

@@ -46,7 +46,10 @@ struct EscShape {
 };
 
 using EscSmall = EscShape<128, 1024, 1024>;
-using EscLarge = EscShape<512, 13312, 2560>;
+using EscMid = EscShape<256, 4096, 1280>;     // 75,968 B numeric: three CTAs per SM
+using EscLarge = EscShape<512, 13312, 2560>;  // 223,424 B numeric: one CTA per SM
+
+constexpr int kUnroll = 4;  // chunks (expansion) or products (fold) with loads in flight together
 
 // Smallest t in [0, n) with incl[t] > p (incl non-decreasing, incl[n-1] > p).
 __device__ __forceinline__ int esc_owner(const int *incl, int n, int p)
@@ -205,17 +208,32 @@ __global__ void __launch_bounds__(Shape::kThreads) k_esc_rows(SpgemmArgs<T> g, c
             if (tid == 0) s_count = 0;
             __syncthreads();
             int cnt = 0;
-            for (int c = warp * 32; c < flop; c += NT) {
-                int o, k;
-                if (!esc_expand_chunk(s_incl, s_b0, lenA, flop, c, &o, &k)) continue;
-                const int col = __ldg(g.bcol + k);
-                if ((unsigned)col >= (unsigned)g.N) {
-                    atomicOr(&g.info->flags, kErrBadColumn);
-                    continue;
+            // kUnroll chunks per round: their column loads are all in flight before the
+            // first claim
+            for (int c0 = warp * 32; c0 < flop; c0 += kUnroll * NT) {
+                int kk[kUnroll];
+                bool v[kUnroll];
+#pragma unroll
+                for (int u = 0; u < kUnroll; ++u) {
+                    const int c = c0 + u * NT;
+                    int o = 0;
+                    kk[u] = 0;
+                    v[u] = c < flop ? esc_expand_chunk(s_incl, s_b0, lenA, flop, c, &o, &kk[u]) : false;
                 }
-                bool is_new = false;
-                table_claim(table, col, log_ts, &is_new, &g.info->flags);
-                cnt += is_new ? 1 : 0;
+                int col[kUnroll];
+#pragma unroll
+                for (int u = 0; u < kUnroll; ++u) col[u] = v[u] ? __ldg(g.bcol + kk[u]) : 0;
+#pragma unroll
+                for (int u = 0; u < kUnroll; ++u) {
+                    if (!v[u]) continue;
+                    if ((unsigned)col[u] >= (unsigned)g.N) {
+                        atomicOr(&g.info->flags, kErrBadColumn);
+                        continue;
+                    }
+                    bool is_new = false;
+                    table_claim(table, col[u], log_ts, &is_new, &g.info->flags);
+                    cnt += is_new ? 1 : 0;
+                }
             }
             cnt = (int)__reduce_add_sync(kFull, (unsigned)cnt);
             if (lane == 0 && cnt) atomicAdd(&s_count, cnt);
@@ -230,12 +248,27 @@ __global__ void __launch_bounds__(Shape::kThreads) k_esc_rows(SpgemmArgs<T> g, c
             const int off = __ldg(g.c_rpt + r);
             const int n_expect = __ldg(g.c_rpt + r + 1) - off;
             const int n = flop;
-            for (int c = warp * 32; c < n; c += NT) {
-                int o, k;
-                if (esc_expand_chunk(s_incl, s_b0, lenA, n, c, &o, &k)) {
-                    key0[c + lane] = (unsigned)__ldg(g.bcol + k);
-                    id0[c + lane] = (unsigned short)(c + lane);
-                    own[c + lane] = (unsigned short)o;
+            for (int c0 = warp * 32; c0 < n; c0 += kUnroll * NT) {
+                int oo[kUnroll], kk[kUnroll];
+                bool v[kUnroll];
+#pragma unroll
+                for (int u = 0; u < kUnroll; ++u) {
+                    const int c = c0 + u * NT;
+                    oo[u] = 0;
+                    kk[u] = 0;
+                    v[u] = c < n ? esc_expand_chunk(s_incl, s_b0, lenA, n, c, &oo[u], &kk[u]) : false;
+                }
+                unsigned key[kUnroll];
+#pragma unroll
+                for (int u = 0; u < kUnroll; ++u) key[u] = v[u] ? (unsigned)__ldg(g.bcol + kk[u]) : 0u;
+#pragma unroll
+                for (int u = 0; u < kUnroll; ++u) {
+                    const int i = c0 + u * NT + lane;
+                    if (v[u]) {
+                        key0[i] = key[u];
+                        id0[i] = (unsigned short)i;
+                        own[i] = (unsigned short)oo[u];
+                    }
                 }
             }
             __syncthreads();
@@ -325,15 +358,37 @@ __global__ void __launch_bounds__(Shape::kThreads) k_esc_rows(SpgemmArgs<T> g, c
             __syncthreads();
             // heads are processed thread-strided, so neighbouring threads work on
             // neighbouring runs and their loads and C stores coalesce
+            // A run is folded kUnroll products at a time: the operands of a batch are
+            // all loaded before its first FMA, so a run of length L waits on memory
+            // ceil(L / kUnroll) times rather than L times.
             for (int i = tid; i < n; i += NT) {
                 const unsigned key = kin[i];
                 if (i > 0 && kin[i - 1] == key) continue;
                 S s = AccT::zero();
-                for (int t = i; t < n && kin[t] == key; ++t) {
-                    const int q = iin[t];
-                    const int o = own[q];
-                    const int k = s_b0[o] + q - (o ? s_incl[o - 1] : 0);
-                    s = AccT::step(s, __ldg(g.aval + a0 + o), __ldg(g.bval + k));
+                bool more = true;
+                for (int t = i; more; t += kUnroll) {
+                    T av[kUnroll], bv[kUnroll];
+                    bool v[kUnroll];
+                    bool run = true;
+#pragma unroll
+                    for (int u = 0; u < kUnroll; ++u) {
+                        const int tt = t + u;
+                        run = run && tt < n && kin[tt] == key;
+                        v[u] = run;
+                        av[u] = T(0);
+                        bv[u] = T(0);
+                        if (run) {
+                            const int q = iin[tt];
+                            const int o = own[q];
+                            const int k = s_b0[o] + q - (o ? s_incl[o - 1] : 0);
+                            av[u] = __ldg(g.aval + a0 + o);
+                            bv[u] = __ldg(g.bval + k);
+                        }
+                    }
+#pragma unroll
+                    for (int u = 0; u < kUnroll; ++u)
+                        if (v[u]) s = AccT::step(s, av[u], bv[u]);
+                    more = v[kUnroll - 1];
                 }
                 const int hp = (int)hpos[i];
                 if (hp < n_expect) {
@@ -347,38 +402,63 @@ __global__ void __launch_bounds__(Shape::kThreads) k_esc_rows(SpgemmArgs<T> g, c
     if constexpr (!kNum) block_add_u64(nnz_acc, &g.info->total_nnz);
 }
 
-// Numeric re-binning of the E1 rows by their output size (known after the symbolic
-// phase): rows with at most kSplitNnz outputs go to the warp-hash numeric kernel (few
-// outputs per product: hashing beats sorting every product), the rest stay with
-// expand/sort/compress.  Counts go to out_counts[0..1] on the device.
-constexpr int kSplitNnz = 256;
-
-static __global__ void k_split_by_nnz(const int *__restrict__ list, const int *count_ptr, const int *__restrict__ c_rpt,
-                                      int *hash_list, int *esc_list, int *out_counts)
+// Device-side re-binning of a class list into kWays sub-lists (out + w*stride), with
+// the row counts added to out_counts[w].  Row order inside a sub-list follows the
+// warp-aggregated atomics, which is fine: every sub-list kernel schedules rows itself.
+template <int kWays, typename Pick>
+__global__ void k_split_list(const int *__restrict__ list, const int *count_ptr, Pick pick, int *out, int stride,
+                             int *out_counts)
 {
     const int count = *count_ptr;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i - (int)threadIdx.x < count; i += gridDim.x * blockDim.x) {
+    const int lane = lane_id();
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i - lane < count; i += gridDim.x * blockDim.x) {
         const bool in = i < count;
-        int r = 0;
-        bool small = false;
+        int r = 0, w = -1;
         if (in) {
             r = list[i];
-            small = c_rpt[r + 1] - c_rpt[r] <= kSplitNnz;
+            w = pick(r);
         }
-        const unsigned ms = __ballot_sync(kFull, in && small);
-        const unsigned ml = __ballot_sync(kFull, in && !small);
-        const int lane = lane_id();
-        int bs = 0, bl = 0;
-        if (lane == 0) {
-            if (ms) bs = atomicAdd(&out_counts[0], __popc(ms));
-            if (ml) bl = atomicAdd(&out_counts[1], __popc(ml));
+#pragma unroll
+        for (int c = 0; c < kWays; ++c) {
+            const unsigned m = __ballot_sync(kFull, w == c);
+            if (!m) continue;
+            int b = 0;
+            if (lane == 0) b = atomicAdd(&out_counts[c], __popc(m));
+            b = __shfl_sync(kFull, b, 0);
+            if (w == c) out[(size_t)c * stride + b + __popc(m & lanemask_lt())] = r;
         }
-        bs = __shfl_sync(kFull, bs, 0);
-        bl = __shfl_sync(kFull, bl, 0);
-        if (in && small) hash_list[bs + __popc(ms & lanemask_lt())] = r;
-        if (in && !small) esc_list[bl + __popc(ml & lanemask_lt())] = r;
     }
 }
+
+// Numeric re-binning of the E1 rows by their output size (known after the symbolic
+// phase): 0 = warp sort (at most kWsortFlopMax products, fewer than two products per
+// output), 1 = warp hash (at most kSplitNnz outputs: hashing folds the many products
+// per output cheaply), 2 = expand/sort/compress.
+constexpr int kSplitNnz = 256;
+
+struct PickE1 {
+    const int *c_rpt;
+    const int *row_flop;
+    int sort_flop_max;
+    __device__ int operator()(int r) const
+    {
+        const int nnz = c_rpt[r + 1] - c_rpt[r];
+        const int f = row_flop[r];
+        if (f <= sort_flop_max && f < 2 * nnz) return 0;
+        return nnz <= kSplitNnz ? 1 : 2;
+    }
+};
+
+// E2 rows by size: 0 = mid shape (EscMid), 1 = large shape (EscLarge).
+struct PickE2 {
+    const int *arpt;
+    const int *row_flop;
+    __device__ int operator()(int r) const
+    {
+        const bool mid = row_flop[r] <= EscMid::kProducts && arpt[r + 1] - arpt[r] <= EscMid::kAEntries;
+        return mid ? 0 : 1;
+    }
+};
 
 // Orders a class list by product count, largest first, so that with dynamic row
 // scheduling the longest rows start first (longest-processing-time order).  One CTA,

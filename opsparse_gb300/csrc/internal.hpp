@@ -36,6 +36,11 @@ struct ops_handle_s {
     cudaStream_t side[kNumClasses] = {};
     cudaEvent_t ev_fork = nullptr;
     cudaEvent_t ev_join[kNumClasses] = {};
+    // extra streams for the second kernel of a re-binned class (E1 numeric, E2)
+    static constexpr int kNumExtra = 2;
+    cudaStream_t side_x[kNumExtra] = {};
+    cudaEvent_t ev_x_fork[kNumExtra] = {};
+    cudaEvent_t ev_x_join[kNumExtra] = {};
     static constexpr int kNumEv = 8;
     cudaEvent_t ev_t[kNumEv] = {};
     cudaEvent_t ev_k[2][kNumClasses][2] = {};  // [phase][class][start, end]

@@ -23,6 +23,7 @@
 #include <string>
 
 #include "esc.cuh"
+#include "wsort.cuh"
 #include "internal.hpp"
 #include "opsparse_gb300.h"
 
@@ -56,6 +57,19 @@ void set_smem_attrs()
                          (int)EscSmall::kSymbolicSmem);
     cudaFuncSetAttribute(k_esc_rows<EscLarge, false, T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)EscLarge::kSymbolicSmem);
+    cudaFuncSetAttribute(k_esc_rows<EscMid, true, T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)EscMid::kNumericSmem);
+    cudaFuncSetAttribute(k_esc_rows<EscMid, false, T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)EscMid::kSymbolicSmem);
+    cudaFuncSetAttribute(k_wsort_rows<4, true, T, unsigned>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)WsortShape<4>::smem<true, T, unsigned>());
+    cudaFuncSetAttribute(k_wsort_rows<4, true, T, unsigned long long>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)WsortShape<4>::smem<true, T, unsigned long long>());
+    cudaFuncSetAttribute(k_wsort_rows<16, true, T, unsigned>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)WsortShape<16>::smem<true, T, unsigned>());
+    cudaFuncSetAttribute(k_wsort_rows<16, true, T, unsigned long long>,
+                         cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)WsortShape<16>::smem<true, T, unsigned long long>());
 }
 
 int ensure_ws(ops_handle_s *h, int M, cudaStream_t st)
@@ -63,8 +77,9 @@ int ensure_ws(ops_handle_s *h, int M, cudaStream_t st)
     if (h->ws && h->ws_M >= M) return OPS_OK;
     size_t cub_bytes = 0;
     OPS_CUDA(h, cub::DeviceScan::ExclusiveSum(nullptr, cub_bytes, (int *)nullptr, (int *)nullptr, M + 1, st));
-    // one list per class plus two for the numeric re-binning of E1 rows
-    const size_t lists_b = align_up(sizeof(int) * (size_t)(kNumClasses + 2) * (size_t)M, 256);
+    // one list per class, three for the numeric re-binning of E1 rows and two for the
+    // E2 rows by size
+    const size_t lists_b = align_up(sizeof(int) * (size_t)(kNumLists) * (size_t)M, 256);
     const size_t flop_b = align_up(sizeof(int) * (size_t)M, 256);
     const size_t info_b = align_up(sizeof(DevInfo), 256);
     const size_t total = lists_b + flop_b + info_b + align_up(cub_bytes, 256);
@@ -128,23 +143,35 @@ int grid_for(long long work_items, int per_block, int cap)
 }
 
 // Launch the kernels of every non-empty class, each on its own stream forked from `st`
-// and joined back into it.
+// and joined back into it.  A re-binned class (E1 numeric, E2) first splits its list on
+// the device and runs its second kernel on an extra stream forked from the class stream;
+// the class stream joins it again, so the class's events span both kernels.
 template <bool kNum, typename T>
 int launch_classes(ops_handle_s *h, const SpgemmArgs<T> &g, cudaStream_t st)
 {
     OPS_CUDA(h, cudaEventRecord(h->ev_fork, st));
     const int sms = h->num_sms;
+    const size_t M = (size_t)h->plan_M;
+    int *xl = h->lists + (size_t)kNumClasses * M;  // extra lists
+    auto fork_x = [&](int x, cudaStream_t from) -> cudaStream_t {
+        if (cudaEventRecord(h->ev_x_fork[x], from) != cudaSuccess) return nullptr;
+        if (cudaStreamWaitEvent(h->side_x[x], h->ev_x_fork[x], 0) != cudaSuccess) return nullptr;
+        return h->side_x[x];
+    };
+    auto join_x = [&](int x, cudaStream_t into) -> bool {
+        return cudaEventRecord(h->ev_x_join[x], h->side_x[x]) == cudaSuccess &&
+               cudaStreamWaitEvent(into, h->ev_x_join[x], 0) == cudaSuccess;
+    };
     for (int c = 0; c < kNumClasses; ++c) {
         const int n = h->counts[c];
         if (n <= 0) continue;
         if (!kNum && c == kClsR8) continue;  // R8 rows are counted inside k_setup
         cudaStream_t s = h->side[c];
         OPS_CUDA(h, cudaStreamWaitEvent(s, h->ev_fork, 0));
-        const int *list = h->lists + (size_t)c * (size_t)h->plan_M;
-        if (!kNum && (c == kClsE2 || c == kClsD) && n > 1 && n <= kLptMax) {
+        const int *list = h->lists + (size_t)c * M;
+        if (!kNum && c == kClsD && n > 1 && n <= kLptMax) {
             // longest rows first; the numeric phase reuses the ordered list
-            k_sort_heavy_first<<<1, 1024, 0, s>>>(h->lists + (size_t)c * (size_t)h->plan_M, &h->info->counts[c],
-                                                  h->row_flop);
+            k_sort_heavy_first<<<1, 1024, 0, s>>>(h->lists + (size_t)c * M, &h->info->counts[c], h->row_flop);
             OPS_CUDA(h, cudaGetLastError());
             ++h->launches;
         }
@@ -159,10 +186,20 @@ int launch_classes(ops_handle_s *h, const SpgemmArgs<T> &g, cudaStream_t st)
             case kClsR32:
                 k_reg_rows<32, kNum, T><<<grid_for(n, 8, sms * 8), 256, 0, s>>>(g, list, n);
                 break;
-            case kClsW: {
-                k_warp_rows<kNum, T, kWarpTableMax>
-                    <<<grid_for(n, kWarpRowsThreads / 32, sms * 8), kWarpRowsThreads,
-                       warp_rows_smem<kNum, T, kWarpTableMax>(), s>>>(g, list, &h->info->counts[c]);
+            case kClsW: {  // warp sort: products sorted in registers, no table
+                using Sh = WsortShape<4>;
+                const int grid = grid_for(n, Sh::kWarps, sms * 8);
+                if (!kNum) {
+                    k_wsort_rows<4, false, T, unsigned>
+                        <<<grid, Sh::kThreads, Sh::smem<false, T, unsigned>(), s>>>(g, list, &h->info->counts[c]);
+                } else if (g.N <= (1 << (32 - Sh::kIdBits))) {
+                    k_wsort_rows<4, true, T, unsigned>
+                        <<<grid, Sh::kThreads, Sh::smem<true, T, unsigned>(), s>>>(g, list, &h->info->counts[c]);
+                } else {
+                    k_wsort_rows<4, true, T, unsigned long long>
+                        <<<grid, Sh::kThreads, Sh::smem<true, T, unsigned long long>(), s>>>(g, list,
+                                                                                            &h->info->counts[c]);
+                }
                 break;
             }
             case kClsE1: {
@@ -170,28 +207,75 @@ int launch_classes(ops_handle_s *h, const SpgemmArgs<T> &g, cudaStream_t st)
                     k_warp_rows<false, T, 2 * kEsc1FlopMax>
                         <<<grid_for(n, kWarpRowsThreads / 32, sms * 3), kWarpRowsThreads,
                            warp_rows_smem<false, T, 2 * kEsc1FlopMax>(), s>>>(g, list, &h->info->counts[c]);
-                } else {  // re-bin by output size, then hash (few outputs) or expand/sort/compress
-                    int *hash_list = h->lists + (size_t)kNumClasses * (size_t)h->plan_M;
-                    int *esc_list = hash_list + h->plan_M;
-                    k_split_by_nnz<<<grid_for(n, 256, sms * 4), 256, 0, s>>>(list, &h->info->counts[c], g.c_rpt,
-                                                                           hash_list, esc_list, h->info->split);
-                    OPS_CUDA(h, cudaGetLastError());
-                    ++h->launches;
-                    k_warp_rows<true, T, 2 * kSplitNnz>
-                        <<<grid_for(n, kWarpRowsThreads / 32, sms * 4), kWarpRowsThreads,
-                           warp_rows_smem<true, T, 2 * kSplitNnz>(), s>>>(g, hash_list, &h->info->split[0]);
-                    OPS_CUDA(h, cudaGetLastError());
-                    ++h->launches;
-                    k_esc_rows<EscSmall, true, T><<<std::min(n, sms * 8), EscSmall::kThreads,
-                                                   EscSmall::kNumericSmem, s>>>(g, esc_list, &h->info->split[1],
-                                                                                &h->info->next[1][c]);
+                    break;
                 }
+                // re-bin by output size: warp sort / warp hash on this stream,
+                // expand/sort/compress on an extra stream
+                int *sort_list = xl + kXlE1Sort * M;
+                int *hash_list = xl + kXlE1Hash * M;
+                int *esc_list = xl + kXlE1Esc * M;
+                k_split_list<3, PickE1><<<grid_for(n, 256, sms * 4), 256, 0, s>>>(
+                    list, &h->info->counts[c], PickE1{g.c_rpt, g.row_flop, kWsortFlopMax}, sort_list, (int)M,
+                    h->info->split);
+                OPS_CUDA(h, cudaGetLastError());
+                ++h->launches;
+                cudaStream_t sx = fork_x(0, s);
+                if (!sx) return fail(h, OPS_CUDA_ERROR, "stream fork failed");
+                k_esc_rows<EscSmall, true, T><<<std::min(n, sms * 8), EscSmall::kThreads, EscSmall::kNumericSmem, sx>>>(
+                    g, esc_list, &h->info->split[2], &h->info->next[1][c]);
+                OPS_CUDA(h, cudaGetLastError());
+                ++h->launches;
+                if (!join_x(0, s)) return fail(h, OPS_CUDA_ERROR, "stream join failed");
+                using Sh = WsortShape<16>;
+                const int sgrid = grid_for(n, Sh::kWarps, sms * 4);
+                if (g.N <= (1 << (32 - Sh::kIdBits))) {
+                    k_wsort_rows<16, true, T, unsigned>
+                        <<<sgrid, Sh::kThreads, Sh::smem<true, T, unsigned>(), s>>>(g, sort_list, &h->info->split[0]);
+                } else {
+                    k_wsort_rows<16, true, T, unsigned long long>
+                        <<<sgrid, Sh::kThreads, Sh::smem<true, T, unsigned long long>(), s>>>(g, sort_list,
+                                                                                              &h->info->split[0]);
+                }
+                OPS_CUDA(h, cudaGetLastError());
+                ++h->launches;
+                k_warp_rows<true, T, 2 * kSplitNnz>
+                    <<<grid_for(n, kWarpRowsThreads / 32, sms * 4), kWarpRowsThreads,
+                       warp_rows_smem<true, T, 2 * kSplitNnz>(), s>>>(g, hash_list, &h->info->split[1]);
                 break;
             }
             case kClsE2: {
-                const size_t smem = kNum ? EscLarge::kNumericSmem : EscLarge::kSymbolicSmem;
-                k_esc_rows<EscLarge, kNum, T><<<std::min(n, sms), EscLarge::kThreads, smem, s>>>(
-                    g, list, &h->info->counts[c], &h->info->next[kNum][c]);
+                // mid shape (3 CTAs per SM) on this stream, large shape (1 per SM) on an
+                // extra stream; the split and the longest-first order are made once, by
+                // the symbolic phase, and reused by numeric
+                int *mid_list = xl + kXlE2Mid * M;
+                int *large_list = xl + kXlE2Large * M;
+                if (!kNum) {
+                    k_split_list<2, PickE2><<<grid_for(n, 256, sms * 4), 256, 0, s>>>(
+                        list, &h->info->counts[c], PickE2{g.arpt, g.row_flop}, mid_list, (int)M, h->info->split2);
+                    OPS_CUDA(h, cudaGetLastError());
+                    ++h->launches;
+                }
+                cudaStream_t sx = fork_x(1, s);
+                if (!sx) return fail(h, OPS_CUDA_ERROR, "stream fork failed");
+                if (!kNum && n > 1) {
+                    k_sort_heavy_first<<<1, 1024, 0, sx>>>(large_list, &h->info->split2[1], h->row_flop);
+                    OPS_CUDA(h, cudaGetLastError());
+                    ++h->launches;
+                }
+                const size_t lsmem = kNum ? EscLarge::kNumericSmem : EscLarge::kSymbolicSmem;
+                k_esc_rows<EscLarge, kNum, T><<<std::min(n, sms), EscLarge::kThreads, lsmem, sx>>>(
+                    g, large_list, &h->info->split2[1], &h->info->next[kNum][c]);
+                OPS_CUDA(h, cudaGetLastError());
+                ++h->launches;
+                if (!join_x(1, s)) return fail(h, OPS_CUDA_ERROR, "stream join failed");
+                if (!kNum && n > 1) {
+                    k_sort_heavy_first<<<1, 1024, 0, s>>>(mid_list, &h->info->split2[0], h->row_flop);
+                    OPS_CUDA(h, cudaGetLastError());
+                    ++h->launches;
+                }
+                const size_t msmem = kNum ? EscMid::kNumericSmem : EscMid::kSymbolicSmem;
+                k_esc_rows<EscMid, kNum, T><<<std::min(n, sms * 3), EscMid::kThreads, msmem, s>>>(
+                    g, mid_list, &h->info->split2[0], &h->info->next_mid[kNum]);
                 break;
             }
             case kClsD: {
@@ -305,6 +389,7 @@ int run_numeric(ops_handle_s *h, const Mat &A, const Mat &B, const int *c_rpt, i
     OPS_CUDA(h, cudaMemsetAsync(&h->info->flags, 0, sizeof(int), st));
     OPS_CUDA(h, cudaMemsetAsync(h->info->next[1], 0, sizeof(h->info->next[1]), st));
     OPS_CUDA(h, cudaMemsetAsync(h->info->split, 0, sizeof(h->info->split), st));
+    OPS_CUDA(h, cudaMemsetAsync(&h->info->next_mid[1], 0, sizeof(int), st));
     SpgemmArgs<T> g{};
     g.arpt = A.rpt;
     g.acol = A.col;
@@ -428,6 +513,11 @@ int ops_handle_create(ops_handle_t *out)
         e = cudaStreamCreateWithFlags(&h->side[c], cudaStreamNonBlocking);
         if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->ev_join[c], cudaEventDisableTiming);
     }
+    for (int x = 0; x < ops_handle_s::kNumExtra && e == cudaSuccess; ++x) {
+        e = cudaStreamCreateWithFlags(&h->side_x[x], cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->ev_x_fork[x], cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->ev_x_join[x], cudaEventDisableTiming);
+    }
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming);
     for (int i = 0; i < ops_handle_s::kNumEv && e == cudaSuccess; ++i) e = cudaEventCreate(&h->ev_t[i]);
     for (int ph = 0; ph < 2 && e == cudaSuccess; ++ph)
@@ -457,6 +547,11 @@ int ops_handle_destroy(ops_handle_t h)
     for (int c = 0; c < kNumClasses; ++c) {
         if (h->side[c]) cudaStreamDestroy(h->side[c]);
         if (h->ev_join[c]) cudaEventDestroy(h->ev_join[c]);
+    }
+    for (int x = 0; x < ops_handle_s::kNumExtra; ++x) {
+        if (h->side_x[x]) cudaStreamDestroy(h->side_x[x]);
+        if (h->ev_x_fork[x]) cudaEventDestroy(h->ev_x_fork[x]);
+        if (h->ev_x_join[x]) cudaEventDestroy(h->ev_x_join[x]);
     }
     if (h->ev_fork) cudaEventDestroy(h->ev_fork);
     for (int i = 0; i < ops_handle_s::kNumEv; ++i)
@@ -523,6 +618,23 @@ int ops_handle_set_output_malloc(ops_handle_t h, int use_cuda_malloc)
 }
 
 const char *ops_handle_last_error(ops_handle_t h) { return h ? h->last_error.c_str() : "null handle"; }
+
+int ops_handle_subclass_rows(ops_handle_t h, int32_t *out, int n)
+{
+    if (!h || !out || n < 0) return OPS_INVALID_ARGUMENT;
+    int v[5] = {};
+    if (h->info) {
+        DevInfo d{};
+        OPS_CUDA(h, cudaMemcpy(&d, h->info, sizeof(DevInfo), cudaMemcpyDeviceToHost));
+        v[0] = d.split[0];
+        v[1] = d.split[1];
+        v[2] = d.split[2];
+        v[3] = d.split2[0];
+        v[4] = d.split2[1];
+    }
+    for (int i = 0; i < n && i < 5; ++i) out[i] = v[i];
+    return OPS_OK;
+}
 
 int ops_spgemm_symbolic(ops_handle_t h, int32_t rows_a, int32_t cols_a, int32_t cols_b, const int32_t *a_rpt,
                         const int32_t *a_col, int64_t a_nnz, const int32_t *b_rpt, const int32_t *b_col, int64_t b_nnz,

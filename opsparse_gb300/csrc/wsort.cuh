@@ -1,0 +1,271 @@
+// wsort.cuh — one warp per row, no hash table: expand the row's products into shared
+// memory, sort (column, product index) keys in registers with a warp bitonic network,
+// fold every run of equal columns in ascending product order, and write C in column
+// order.  Used for rows whose products mostly land in distinct columns (web-like rows:
+// nnz(C row) close to the product count).  For them a hash table costs a probe per
+// product and still needs a sort of the table afterwards; sorting the products once
+// does strictly less.  Replaces, for those rows, OpSparse's shared-hash numeric and
+// symbolic kernels of the small and middle bins (kernels/numeric.cuh:109-205,
+// kernels/symbolic.cuh:74-130).
+//
+// Keys: numeric packs (column << kIdBits) | product index, so equal columns sort in
+// ascending product order (= ascending j, the oracle's order) and the sort needs no
+// stability.  Symbolic sorts bare columns and counts the distinct ones.
+#pragma once
+
+#include "kernels.cuh"
+
+namespace opsg {
+
+constexpr int kWsortFlopMax = 512;  // largest row of the 16-per-lane variant
+
+// Shared-memory index of element e with one pad word per 32: the blocked register layout
+// (lane l holds elements l*PER .. l*PER+PER-1) then reads and writes without bank
+// conflicts, and so does the expansion's contiguous stores.
+__device__ __forceinline__ int wpad(int e) { return e + (e >> 5); }
+
+// Ascending bitonic sort of the 32*PER keys held blocked across the warp.  Partner
+// distances of PER and above are exchanged with shuffles, smaller ones in registers.
+template <int PER, typename KT>
+__device__ __forceinline__ void warp_bitonic_blocked(KT (&x)[PER])
+{
+    const int lane = lane_id();
+    constexpr int n = 32 * PER;
+#pragma unroll
+    for (int k = 2; k <= n; k <<= 1) {
+#pragma unroll
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            if (j >= PER) {
+                const bool lower = ((lane * PER) & j) == 0;
+#pragma unroll
+                for (int i = 0; i < PER; ++i) {
+                    const bool asc = ((lane * PER + i) & k) == 0;
+                    const KT y = __shfl_xor_sync(kFull, x[i], j / PER);
+                    x[i] = (lower == asc) ? (x[i] < y ? x[i] : y) : (x[i] < y ? y : x[i]);
+                }
+            } else {
+#pragma unroll
+                for (int i = 0; i < PER; ++i) {
+                    if ((i & j) == 0) {
+                        const bool asc = ((lane * PER + i) & k) == 0;
+                        const KT a = x[i], b = x[i | j];
+                        const bool sw = asc ? (b < a) : (a < b);
+                        x[i] = sw ? b : a;
+                        x[i | j] = sw ? a : b;
+                    }
+                }
+            }
+        }
+    }
+}
+
+template <int PMAX>
+struct WsortShape {
+    static constexpr int kMax = 32 * PMAX;                     // products per row, at most
+    static constexpr int kWarps = PMAX <= 4 ? 8 : 4;           // warps per CTA
+    static constexpr int kThreads = 32 * kWarps;
+    static constexpr int kIdBits = PMAX <= 4 ? 7 : (PMAX <= 8 ? 8 : 9);
+    static constexpr int kKeySlots = kMax + kMax / 32;         // padded key array
+    static constexpr int kHeadSlots = kMax + 32;               // run heads + end marker
+
+    template <bool kNum, typename T, typename KT>
+    static constexpr size_t per_warp()
+    {
+        return (sizeof(KT) * kKeySlots + 15) / 16 * 16 + (kNum ? sizeof(int) * kHeadSlots + 2 * sizeof(T) * kMax : 0);
+    }
+    template <bool kNum, typename T, typename KT>
+    static constexpr size_t smem()
+    {
+        return (size_t)kWarps * per_warp<kNum, T, KT>();
+    }
+};
+
+// Sort the row's `flop` keys (already in skey at padded positions), then count (symbolic)
+// or fold and write (numeric) the runs.  Returns the number of distinct columns.
+template <int PER, int kIdBits, bool kNum, typename T, typename KT>
+__device__ __forceinline__ int wsort_row(const SpgemmArgs<T> &g, int flop, KT *skey, int *heads, const T *sa,
+                                         const T *sb, int off, int n_expect)
+{
+    using AccT = Acc<T>;
+    using S = typename AccT::S;
+    const int lane = lane_id();
+    KT x[PER];
+#pragma unroll
+    for (int i = 0; i < PER; ++i) {
+        const int e = lane * PER + i;
+        x[i] = e < flop ? skey[wpad(e)] : ~KT(0);
+    }
+    warp_bitonic_blocked<PER, KT>(x);
+    const KT before = __shfl_up_sync(kFull, x[PER - 1], 1);
+    unsigned hm = 0;
+    int h = 0;
+#pragma unroll
+    for (int i = 0; i < PER; ++i) {
+        const int e = lane * PER + i;
+        const KT prev = i ? x[i - 1] : before;
+        const bool head = e < flop && (e == 0 || (x[i] >> kIdBits) != (prev >> kIdBits));
+        hm |= head ? (1u << i) : 0u;
+        h += head ? 1 : 0;
+    }
+    int incl = h;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const int t = __shfl_up_sync(kFull, incl, d);
+        if (lane >= d) incl += t;
+    }
+    const int total = __shfl_sync(kFull, incl, 31);
+    if constexpr (kNum) {
+        int pos = incl - h;
+#pragma unroll
+        for (int i = 0; i < PER; ++i) {
+            const int e = lane * PER + i;
+            skey[wpad(e)] = x[i];
+            if ((hm >> i) & 1u) heads[pos++] = e;
+        }
+        if (lane == 0) heads[total] = flop;
+        __syncwarp();
+        constexpr KT kIdMask = (KT(1) << kIdBits) - 1;
+        // heads in lane order: consecutive lanes write consecutive entries of C
+        for (int hh = lane; hh < total; hh += 32) {
+            const int e0 = heads[hh], e1 = heads[hh + 1];
+            const KT k0 = skey[wpad(e0)];
+            S s = AccT::zero();
+            for (int t = e0; t < e1; ++t) {
+                const int pid = (int)(skey[wpad(t)] & kIdMask);
+                s = AccT::step(s, sa[pid], sb[pid]);
+            }
+            if (hh < n_expect) {
+                g.c_col[off + hh] = (int)(k0 >> kIdBits);
+                g.c_val[off + hh] = AccT::fin(s);
+            }
+        }
+        __syncwarp();
+    }
+    return total;
+}
+
+// One warp per listed row (flop <= 32*PMAX).  Rows of at most 128 products sort 128 keys,
+// at most 256 sort 256, the rest 512 (PMAX = 16 only).  The row count is read from
+// device memory, so lists split on the device need no host round trip.
+template <int PMAX, bool kNum, typename T, typename KT>
+__global__ void __launch_bounds__(WsortShape<PMAX>::kThreads) k_wsort_rows(SpgemmArgs<T> g, const int *__restrict__ list,
+                                                                         const int *count_ptr)
+{
+    using Sh = WsortShape<PMAX>;
+    constexpr int kIdBits = kNum ? Sh::kIdBits : 0;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int lane = lane_id();
+    const int warp = threadIdx.x >> 5;
+    unsigned char *base = smem_raw + (size_t)warp * Sh::template per_warp<kNum, T, KT>();
+    KT *skey = reinterpret_cast<KT *>(base);
+    base += (sizeof(KT) * Sh::kKeySlots + 15) / 16 * 16;
+    int *heads = nullptr;
+    T *sa = nullptr, *sb = nullptr;
+    if constexpr (kNum) {
+        sa = reinterpret_cast<T *>(base);
+        sb = sa + Sh::kMax;
+        heads = reinterpret_cast<int *>(sb + Sh::kMax);
+    }
+    const int count = *count_ptr;
+    const long long warp0 = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
+    unsigned long long nnz_acc = 0;
+
+    for (long long it = warp0; it < count; it += nwarps) {
+        const int r = __ldg(list + it);
+        const int a0 = __ldg(g.arpt + r);
+        const int a1 = __ldg(g.arpt + r + 1);
+        const int flop = __ldg(g.row_flop + r);
+        int off = 0, n_expect = 0;
+        if constexpr (kNum) {
+            off = __ldg(g.c_rpt + r);
+            n_expect = __ldg(g.c_rpt + r + 1) - off;
+        }
+        // expansion: windows of 32 A entries, kUnroll chunks of 32 products in flight
+        int wbase = 0;
+        bool bad = false;
+        for (int wa = a0; wa < a1; wa += 32) {
+            const int q = wa + lane;
+            int b0 = 0, bl = 0;
+            T av = T(0);
+            if (q < a1) {
+                const int j = __ldg(g.acol + q);
+                b0 = __ldg(g.brpt + j);
+                bl = __ldg(g.brpt + j + 1) - b0;
+                if constexpr (kNum) av = __ldg(g.aval + q);
+            }
+            int incl = bl;
+#pragma unroll
+            for (int d = 1; d < 32; d <<= 1) {
+                const int t = __shfl_up_sync(kFull, incl, d);
+                if (lane >= d) incl += t;
+            }
+            const int wtot = __shfl_sync(kFull, incl, 31);
+            for (int c = 0; c < wtot; c += 32 * kUnroll) {
+                int kk[kUnroll];
+                T oav[kUnroll];
+                bool v[kUnroll];
+#pragma unroll
+                for (int u = 0; u < kUnroll; ++u) {
+                    const int p = c + u * 32 + lane;
+                    v[u] = p < wtot;
+                    int lo = 0;
+#pragma unroll
+                    for (int step = 16; step >= 1; step >>= 1) {
+                        const int vv = __shfl_sync(kFull, incl, lo + step - 1);
+                        if (vv <= p) lo += step;
+                    }
+                    const int o_incl = __shfl_sync(kFull, incl, lo);
+                    const int o_bl = __shfl_sync(kFull, bl, lo);
+                    const int o_b0 = __shfl_sync(kFull, b0, lo);
+                    oav[u] = kNum ? shfl(av, lo) : T(0);
+                    kk[u] = o_b0 + (p - (o_incl - o_bl));
+                }
+                int col[kUnroll];
+                T bv[kUnroll];
+#pragma unroll
+                for (int u = 0; u < kUnroll; ++u) {
+                    col[u] = v[u] ? __ldg(g.bcol + kk[u]) : 0;
+                    bv[u] = (kNum && v[u]) ? __ldg(g.bval + kk[u]) : T(0);
+                }
+#pragma unroll
+                for (int u = 0; u < kUnroll; ++u) {
+                    const int idx = wbase + c + u * 32 + lane;
+                    if (!v[u] || idx >= Sh::kMax) continue;  // listed rows have flop <= kMax
+                    bad |= (unsigned)col[u] >= (unsigned)g.N;
+                    skey[wpad(idx)] = ((KT)(unsigned)col[u] << kIdBits) | (KT)(kNum ? idx : 0);
+                    if constexpr (kNum) {
+                        sa[idx] = oav[u];
+                        sb[idx] = bv[u];
+                    }
+                }
+            }
+            wbase += wtot;
+        }
+        if (bad) atomicOr(&g.info->flags, kErrBadColumn);
+        __syncwarp();
+        int total;
+        if (flop <= 128) {
+            total = wsort_row<4, kIdBits, kNum, T, KT>(g, flop, skey, heads, sa, sb, off, n_expect);
+        } else if constexpr (PMAX >= 8) {
+            if (flop <= 256)
+                total = wsort_row<8, kIdBits, kNum, T, KT>(g, flop, skey, heads, sa, sb, off, n_expect);
+            else
+                total = wsort_row<PMAX, kIdBits, kNum, T, KT>(g, flop, skey, heads, sa, sb, off, n_expect);
+        } else {
+            total = 0;  // not reached: rows are listed here only if flop <= 32*PMAX
+        }
+        if constexpr (!kNum) {
+            if (lane == 0) {
+                g.c_rpt[r] = total;
+                nnz_acc += (unsigned long long)total;
+            }
+        } else {
+            if (lane == 0 && total != n_expect) atomicOr(&g.info->flags, kErrCountMismatch);
+        }
+        __syncwarp();
+    }
+    if constexpr (!kNum) block_add_u64(nnz_acc, &g.info->total_nnz);
+}
+
+}  // namespace opsg

@@ -87,6 +87,49 @@ def test_class_coverage(cuda, handle):
     assert np.all(seen > 0), seen
 
 
+def test_subclass_coverage(cuda, handle):
+    """The case set reaches every sub-kernel of the re-binned classes (E1 numeric: warp
+    sort, warp hash, expand/sort/compress; E2: mid and large shape)."""
+    seen = {}
+    for case in CASES:
+        run_case(cuda, handle, case, cuda.float64)
+        for k, v in handle.subclass_rows().items():
+            seen[k] = seen.get(k, 0) + v
+    assert all(v > 0 for v in seen.values()), seen
+
+
+def _stretch_columns(case, factor=600):
+    """Same products with B's columns spread over factor*N columns by the strictly
+    increasing map c -> factor*c + c % 7; C is the original C under the same map."""
+    name, a, b, ncols = case
+    f = lambda c: (c.astype(np.int64) * factor + c % 7).astype(np.int32)
+    return (name + "_wide", a, (b[0], f(b[1]), b[2]), int(f(np.array([ncols - 1]))[0]) + 1), f
+
+
+@pytest.mark.parametrize("dtype", ["f64", "f32"])
+def test_wide_columns(cuda, handle, dtype):
+    """More than 2^25 columns: the warp-sort kernels switch to 64-bit (column, product)
+    keys.  Results are the oracle's under the column map."""
+    case, f = _stretch_columns(CASES[2])
+    assert case[3] > (1 << 25)
+    name, a, b, ncols = case
+    orig = CASES[2]
+    if dtype == "f64":
+        rpt, col, val = run_case(cuda, handle, case, cuda.float64)
+        orpt, ocol, oval = oracle.spgemm(*orig[1], *orig[2], orig[3])
+        assert np.array_equal(val.view(np.uint64), oval.view(np.uint64))
+    else:
+        a32 = (a[0], a[1], a[2].astype(np.float32))
+        b32 = (b[0], b[1], b[2].astype(np.float32))
+        rpt, col, val = run_case(cuda, handle, (name, a32, b32, ncols), cuda.float32)
+        orpt, ocol, oval = oracle.spgemm(a[0], a[1], a32[2], orig[2][0], orig[2][1], b32[2], orig[3],
+                                         dtype=np.float32)
+        assert np.array_equal(val.view(np.uint32), oval.view(np.uint32))
+    assert np.array_equal(rpt.astype(np.int64), orpt)
+    assert np.array_equal(col, f(ocol))
+    assert handle.subclass_rows()["e1_sort"] > 0
+
+
 def test_repeat_and_resize(cuda, handle):
     """Workspace reuse across calls of different sizes gives identical results."""
     big = CASES[2]
