@@ -88,6 +88,13 @@ __device__ __forceinline__ uint32_t hash_slot(int key, int log_ts)
     return ((uint32_t)key * 2654435761u) >> (32 - log_ts);
 }
 
+constexpr int ceil_log2_c(int x)
+{
+    int l = 0;
+    while ((1 << l) < x) ++l;
+    return l;
+}
+
 __host__ __device__ __forceinline__ int ceil_log2(int x)
 {
     int l = 0;

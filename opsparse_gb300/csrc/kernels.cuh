@@ -53,6 +53,14 @@ __device__ __forceinline__ unsigned long long warp_sum_u64(unsigned long long v)
     return v;
 }
 
+// Sum of one u64 per thread over the warp, added to *dst by lane 0: no block barrier,
+// so warps of one CTA that finish early do not wait for the others.
+__device__ __forceinline__ void warp_add_u64(unsigned long long v, unsigned long long *dst)
+{
+    v = warp_sum_u64(v);
+    if (lane_id() == 0 && v) atomicAdd(dst, v);
+}
+
 // Sum of one u64 per thread over the block, added to *dst by one thread.  Every thread
 // of the block must call it.
 __device__ __forceinline__ void block_add_u64(unsigned long long v, unsigned long long *dst)
@@ -72,11 +80,13 @@ __device__ __forceinline__ void block_add_u64(unsigned long long v, unsigned lon
 
 // ==================================================================================
 // Setup: per-row product count, validation of A's columns, class assignment, and the
-// scatter of row ids into per-class lists (lists[c * M + i]).  One warp owns 32
-// consecutive rows; rows with more than 8 A entries are summed cooperatively by the
-// warp.  Rows with no products get nnz 0 immediately and join no list.
+// scatter of row ids into per-class lists (lists[c * M + i]).  One thread per row for
+// rows of at most 8 A entries, whose loads are issued all at once (8 column loads, then
+// 16 row-pointer loads); longer rows are summed cooperatively by their warp, 8 loads in
+// flight per lane.  Rows with no products get nnz 0 immediately and join no list.
 // ==================================================================================
 constexpr int kSetupThreads = 512;
+constexpr int kSetupUnroll = 8;
 
 static __global__ void __launch_bounds__(kSetupThreads) k_setup(const int *__restrict__ arpt, const int *__restrict__ acol,
                                                         const int *__restrict__ brpt, const int *__restrict__ bcol,
@@ -84,7 +94,7 @@ static __global__ void __launch_bounds__(kSetupThreads) k_setup(const int *__res
                                                         int *__restrict__ lists, int *__restrict__ c_rownnz,
                                                         DevInfo *info, Thresholds th)
 {
-    __shared__ int s_keys[kSmallFlopMax][kSetupThreads];  // R8 rows: the row's column keys
+    static_assert(kSmallFlopMax == kSetupUnroll, "R8 rows are gathered from the light-row registers");
     __shared__ int s_cnt[kNumClasses];
     __shared__ int s_base[kNumClasses];
     __shared__ unsigned long long s_flop[kSetupThreads / 32];
@@ -106,14 +116,26 @@ static __global__ void __launch_bounds__(kSetupThreads) k_setup(const int *__res
     const int lenA = a1 - a0;
     long long flop = 0;
     bool bad = false;
-    if (in && lenA <= 8) {
-        for (int p = a0; p < a1; ++p) {
-            const int j = __ldg(acol + p);
-            if ((unsigned)j < (unsigned)K) flop += __ldg(brpt + j + 1) - __ldg(brpt + j);
-            else bad = true;
+    const bool light = in && lenA <= kSetupUnroll;
+    int b0[kSetupUnroll], bl[kSetupUnroll];
+    {
+        int jj[kSetupUnroll];
+#pragma unroll
+        for (int u = 0; u < kSetupUnroll; ++u) jj[u] = (light && u < lenA) ? __ldg(acol + a0 + u) : -1;
+#pragma unroll
+        for (int u = 0; u < kSetupUnroll; ++u) {
+            b0[u] = 0;
+            bl[u] = 0;
+            if (jj[u] >= 0 && jj[u] < K) {
+                b0[u] = __ldg(brpt + jj[u]);
+                bl[u] = __ldg(brpt + jj[u] + 1) - b0[u];
+            } else if (light && u < lenA) {
+                bad = true;
+            }
+            flop += bl[u];
         }
     }
-    unsigned heavy = __ballot_sync(kFull, in && lenA > 8);
+    unsigned heavy = __ballot_sync(kFull, in && !light);
     while (heavy) {
         const int t = __ffs(heavy) - 1;
         heavy &= heavy - 1u;
@@ -121,10 +143,23 @@ static __global__ void __launch_bounds__(kSetupThreads) k_setup(const int *__res
         const int h1 = __shfl_sync(kFull, a1, t);
         unsigned long long s = 0;
         bool hb = false;
-        for (int p = h0 + lane; p < h1; p += 32) {
-            const int j = __ldg(acol + p);
-            if ((unsigned)j < (unsigned)K) s += (unsigned long long)(__ldg(brpt + j + 1) - __ldg(brpt + j));
-            else hb = true;
+        for (int p0 = h0; p0 < h1; p0 += 32 * kSetupUnroll) {
+            int jj[kSetupUnroll];
+#pragma unroll
+            for (int u = 0; u < kSetupUnroll; ++u) {
+                const int p = p0 + u * 32 + lane;
+                jj[u] = p < h1 ? __ldg(acol + p) : -1;
+            }
+            int lo[kSetupUnroll], hi[kSetupUnroll];
+#pragma unroll
+            for (int u = 0; u < kSetupUnroll; ++u) {
+                const bool ok = (unsigned)jj[u] < (unsigned)K;
+                hb |= (p0 + u * 32 + lane < h1) && !ok;
+                lo[u] = ok ? __ldg(brpt + jj[u]) : 0;
+                hi[u] = ok ? __ldg(brpt + jj[u] + 1) : 0;
+            }
+#pragma unroll
+            for (int u = 0; u < kSetupUnroll; ++u) s += (unsigned long long)(hi[u] - lo[u]);
         }
         s = warp_sum_u64(s);
         hb = __any_sync(kFull, hb);
@@ -144,21 +179,33 @@ static __global__ void __launch_bounds__(kSetupThreads) k_setup(const int *__res
         if (flop == 0) {
             c_rownnz[r] = 0;
         } else if (!bad && flop <= th.r8 && lenA <= th.r8) {
-            // R8 row: its symbolic phase happens here — gather the <= 8 column keys and
-            // count the distinct ones.  These rows join no list; the numeric phase walks
-            // them in row order (k_small_rows).
+            // R8 row: its symbolic phase happens here.  Product t (t < flop <= 8) is
+            // entry b0[u] + t - pre[u] of the B row of the A entry u that covers it; the
+            // <= 8 column keys are loaded together and the distinct ones counted in
+            // registers.  These rows join no list; the numeric phase walks them in row
+            // order (k_small_rows).
             cls = kClsR8;
-            int n = 0;
-            for (int p = a0; p < a1; ++p) {
-                const int j = __ldg(acol + p);
-                const int q1 = __ldg(brpt + j + 1);
-                for (int q = __ldg(brpt + j); q < q1; ++q) s_keys[n++][threadIdx.x] = __ldg(bcol + q);
+            int kt[kSmallFlopMax];
+#pragma unroll
+            for (int t = 0; t < kSmallFlopMax; ++t) kt[t] = 0;
+            int pre = 0;
+#pragma unroll
+            for (int u = 0; u < kSetupUnroll; ++u) {
+#pragma unroll
+                for (int t = 0; t < kSmallFlopMax; ++t)
+                    if (t >= pre && t < pre + bl[u]) kt[t] = b0[u] + t - pre;
+                pre += bl[u];
             }
-            for (int m = 0; m < n; ++m) {
-                const int km = s_keys[m][threadIdx.x];
-                bool dup = (unsigned)km >= (unsigned)N;
+            int key[kSmallFlopMax];
+#pragma unroll
+            for (int t = 0; t < kSmallFlopMax; ++t) key[t] = t < f32 ? __ldg(bcol + kt[t]) : -1;
+#pragma unroll
+            for (int t = 0; t < kSmallFlopMax; ++t) {
+                if (t >= f32) continue;
+                bool dup = (unsigned)key[t] >= (unsigned)N;
                 if (dup) atomicOr(&s_flags, kErrBadColumn);
-                for (int t = 0; t < m && !dup; ++t) dup = s_keys[t][threadIdx.x] == km;
+#pragma unroll
+                for (int q = 0; q < t; ++q) dup |= key[q] == key[t];
                 small_nnz += dup ? 0u : 1u;
             }
             c_rownnz[r] = (int)small_nnz;
@@ -218,66 +265,106 @@ static __global__ void __launch_bounds__(kSetupThreads) k_setup(const int *__res
 
 // ==================================================================================
 // Numeric phase of the R8 rows (<= 8 products, <= 8 A entries), one thread per row in
-// row order: no list, coalesced row metadata.  The thread gathers its products as
-// (key, a, b) into its own column of shared slots, insertion-sorts them by key — stable,
-// so equal keys keep ascending j — then folds each run with one FMA per product and
-// writes C in column order.
+// row order: no list, coalesced row metadata, nothing in shared memory.  Each level of
+// loads is issued at once (A entries, then B row pointers, then the <= 8 products), the
+// products are sorted in registers by (column, product index) with a 19-comparator
+// network — equal columns keep ascending j — and each run is folded with one FMA per
+// product, so a warp issues at most 8 FMA instructions per 32 rows.
 // ==================================================================================
 constexpr int kSmallThreads = 256;
+
+template <typename K, typename T>
+__device__ __forceinline__ void cmp_swap3(K &ka, T &aa, T &ba, K &kb, T &ab, T &bb)
+{
+    const bool sw = kb < ka;
+    const K k = sw ? kb : ka;
+    kb = sw ? ka : kb;
+    ka = k;
+    const T a = sw ? ab : aa;
+    ab = sw ? aa : ab;
+    aa = a;
+    const T b = sw ? bb : ba;
+    bb = sw ? ba : bb;
+    ba = b;
+}
 
 template <typename T>
 __global__ void __launch_bounds__(kSmallThreads) k_small_rows(SpgemmArgs<T> g, int r8)
 {
     using AccT = Acc<T>;
-    __shared__ int s_key[kSmallFlopMax][kSmallThreads];
-    __shared__ T s_a[kSmallFlopMax][kSmallThreads];
-    __shared__ T s_b[kSmallFlopMax][kSmallThreads];
-    const int t = threadIdx.x;
-    for (int r = blockIdx.x * kSmallThreads + t; r < g.M; r += gridDim.x * kSmallThreads) {
+    constexpr int U = kSmallFlopMax;
+    static_assert(U == 8, "the sorting network is for 8 keys");
+    for (int r = blockIdx.x * kSmallThreads + threadIdx.x; r < g.M; r += gridDim.x * kSmallThreads) {
         const int flop = __ldg(g.row_flop + r);
         const int a0 = __ldg(g.arpt + r);
-        const int a1 = __ldg(g.arpt + r + 1);
-        if (flop == 0 || flop > r8 || a1 - a0 > r8) continue;
-        int n = 0;
-        for (int p = a0; p < a1; ++p) {
-            const int j = __ldg(g.acol + p);
-            const T a = __ldg(g.aval + p);
-            const int q1 = __ldg(g.brpt + j + 1);
-            for (int q = __ldg(g.brpt + j); q < q1; ++q) {
-                s_key[n][t] = __ldg(g.bcol + q);
-                s_a[n][t] = a;
-                s_b[n][t] = __ldg(g.bval + q);
-                ++n;
-            }
+        const int lenA = __ldg(g.arpt + r + 1) - a0;
+        if (flop == 0 || flop > r8 || lenA > r8) continue;
+        int jj[U];
+        T av[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            jj[u] = u < lenA ? __ldg(g.acol + a0 + u) : 0;
+            av[u] = u < lenA ? __ldg(g.aval + a0 + u) : T(0);
         }
-        for (int m = 1; m < n; ++m) {
-            const int k = s_key[m][t];
-            const T a = s_a[m][t], b = s_b[m][t];
-            int i = m - 1;
-            while (i >= 0 && s_key[i][t] > k) {
-                s_key[i + 1][t] = s_key[i][t];
-                s_a[i + 1][t] = s_a[i][t];
-                s_b[i + 1][t] = s_b[i][t];
-                --i;
-            }
-            s_key[i + 1][t] = k;
-            s_a[i + 1][t] = a;
-            s_b[i + 1][t] = b;
+        int b0[U], bl[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            b0[u] = u < lenA ? __ldg(g.brpt + jj[u]) : 0;
+            bl[u] = u < lenA ? __ldg(g.brpt + jj[u] + 1) - b0[u] : 0;
         }
+        // product t is entry b0[u] + t - pre[u] of the B row of the A entry u covering it
+        int kt[U];
+        T at[U];
+#pragma unroll
+        for (int t = 0; t < U; ++t) {
+            kt[t] = 0;
+            at[t] = T(0);
+        }
+        int pre = 0;
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+#pragma unroll
+            for (int t = 0; t < U; ++t) {
+                if (t >= pre && t < pre + bl[u]) {
+                    kt[t] = b0[u] + t - pre;
+                    at[t] = av[u];
+                }
+            }
+            pre += bl[u];
+        }
+        unsigned long long key[U];
+        T bt[U];
+#pragma unroll
+        for (int t = 0; t < U; ++t) {
+            const bool v = t < flop;
+            key[t] = v ? (((unsigned long long)(unsigned)__ldg(g.bcol + kt[t]) << 3) | (unsigned)t) : ~0ull;
+            bt[t] = v ? __ldg(g.bval + kt[t]) : T(0);
+        }
+#define OPSG_CS(i, j) cmp_swap3(key[i], at[i], bt[i], key[j], at[j], bt[j])
+        OPSG_CS(0, 2); OPSG_CS(1, 3); OPSG_CS(4, 6); OPSG_CS(5, 7);
+        OPSG_CS(0, 4); OPSG_CS(1, 5); OPSG_CS(2, 6); OPSG_CS(3, 7);
+        OPSG_CS(0, 1); OPSG_CS(2, 3); OPSG_CS(4, 5); OPSG_CS(6, 7);
+        OPSG_CS(2, 4); OPSG_CS(3, 5);
+        OPSG_CS(1, 4); OPSG_CS(3, 6);
+        OPSG_CS(1, 2); OPSG_CS(3, 4); OPSG_CS(5, 6);
+#undef OPSG_CS
         const int off = __ldg(g.c_rpt + r);
         const int n_expect = __ldg(g.c_rpt + r + 1) - off;
         typename AccT::S acc = AccT::zero();
         int pos = 0;
-        for (int m = 0; m < n; ++m) {
-            const int k = s_key[m][t];
-            acc = AccT::step(acc, s_a[m][t], s_b[m][t]);
-            if (m + 1 == n || s_key[m + 1][t] != k) {
-                if (pos < n_expect) {
-                    g.c_col[off + pos] = k;
-                    g.c_val[off + pos] = AccT::fin(acc);
+#pragma unroll
+        for (int m = 0; m < U; ++m) {
+            if (m < flop) {
+                acc = AccT::step(acc, at[m], bt[m]);
+                const bool last = m + 1 == flop || (m + 1 < U && (key[m + 1] >> 3) != (key[m] >> 3));
+                if (last) {
+                    if (pos < n_expect) {
+                        g.c_col[off + pos] = (int)(key[m] >> 3);
+                        g.c_val[off + pos] = AccT::fin(acc);
+                    }
+                    ++pos;
+                    acc = AccT::zero();
                 }
-                ++pos;
-                acc = AccT::zero();
             }
         }
         if (pos != n_expect) atomicOr(&g.info->flags, kErrCountMismatch);
@@ -368,7 +455,7 @@ __global__ void __launch_bounds__(256) k_reg_rows(SpgemmArgs<T> g, const int *__
             }
         }
     }
-    if constexpr (!kNum) block_add_u64(nnz_acc, &g.info->total_nnz);
+    if constexpr (!kNum) warp_add_u64(nnz_acc, &g.info->total_nnz);
 }
 
 // ==================================================================================
@@ -382,6 +469,7 @@ __global__ void __launch_bounds__(256) k_reg_rows(SpgemmArgs<T> g, const int *__
 // at its rank among the row's columns.
 // ==================================================================================
 constexpr int kWarpRowsThreads = 256;
+constexpr int kCountUnroll = 4;  // symbolic: chunks whose column loads are issued together
 
 template <bool kNum, typename T, int TMAX>
 constexpr size_t warp_rows_smem()
@@ -426,7 +514,50 @@ __global__ void __launch_bounds__(kWarpRowsThreads) k_warp_rows(SpgemmArgs<T> g,
         __syncwarp();
         int cnt = 0;
         const int row_products = kNum ? __ldg(g.row_flop + r) : n_expect;
-        if (row_products >= 16 * (a1 - a0)) {
+        if constexpr (!kNum) {
+            // counting is order-free: kUnroll chunks of 32 products have their column
+            // loads in flight together before the claims
+            for (int wa = a0; wa < a1; wa += 32) {
+                const int q = wa + lane;
+                int b0 = 0, bl = 0;
+                if (q < a1) {
+                    const int j = __ldg(g.acol + q);
+                    b0 = __ldg(g.brpt + j);
+                    bl = __ldg(g.brpt + j + 1) - b0;
+                }
+                int incl = bl;
+#pragma unroll
+                for (int d = 1; d < 32; d <<= 1) {
+                    const int t = __shfl_up_sync(kFull, incl, d);
+                    if (lane >= d) incl += t;
+                }
+                const int wtot = __shfl_sync(kFull, incl, 31);
+                for (int c = 0; c < wtot; c += 32 * kCountUnroll) {
+                    int col[kCountUnroll];
+#pragma unroll
+                    for (int u = 0; u < kCountUnroll; ++u) {
+                        const int p = c + u * 32 + lane;
+                        int lo = 0;
+#pragma unroll
+                        for (int step = 16; step >= 1; step >>= 1) {
+                            const int vv = __shfl_sync(kFull, incl, lo + step - 1);
+                            if (vv <= p) lo += step;
+                        }
+                        const int o_incl = __shfl_sync(kFull, incl, lo);
+                        const int o_bl = __shfl_sync(kFull, bl, lo);
+                        const int o_b0 = __shfl_sync(kFull, b0, lo);
+                        col[u] = p < wtot ? __ldg(g.bcol + o_b0 + (p - (o_incl - o_bl))) : kEmpty;
+                    }
+#pragma unroll
+                    for (int u = 0; u < kCountUnroll; ++u) {
+                        if (col[u] == kEmpty) continue;
+                        bool is_new = false;
+                        table_claim(keys, col[u], log_ts, &is_new, &g.info->flags);
+                        cnt += is_new ? 1 : 0;
+                    }
+                }
+            }
+        } else if (row_products >= 16 * (a1 - a0)) {
             // long B rows: one B row per step, every lane owns a distinct key
             warp_rowwise_products<kNum, T>(a0, a1, g.acol, g.aval, g.brpt, [&](bool valid, int k, T av) {
                 if (valid) {
@@ -523,7 +654,7 @@ __global__ void __launch_bounds__(kWarpRowsThreads) k_warp_rows(SpgemmArgs<T> g,
             __syncwarp();
         }
     }
-    if constexpr (!kNum) block_add_u64(nnz_acc, &g.info->total_nnz);
+    if constexpr (!kNum) warp_add_u64(nnz_acc, &g.info->total_nnz);
 }
 
 // ==================================================================================
@@ -729,7 +860,7 @@ __global__ void __launch_bounds__(kDenseRowsThreads) k_dense_rows(SpgemmArgs<T> 
             __syncthreads();
         }
     }
-    if constexpr (!kNum) block_add_u64(nnz_acc, &g.info->total_nnz);
+    if constexpr (!kNum) warp_add_u64(nnz_acc, &g.info->total_nnz);
 }
 
 }  // namespace opsg

@@ -22,7 +22,7 @@
 #include <new>
 #include <string>
 
-#include "esc.cuh"
+#include "besc.cuh"
 #include "wsort.cuh"
 #include "internal.hpp"
 #include "opsparse_gb300.h"
@@ -40,27 +40,53 @@ struct Mat {
     const void *val;
 };
 
+template <typename Shape, typename T>
+void set_besc_attrs()
+{
+    cudaFuncSetAttribute(k_besc_rows<Shape, true, T, unsigned>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)Shape::template smem<true, unsigned>());
+    cudaFuncSetAttribute(k_besc_rows<Shape, true, T, unsigned long long>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)Shape::template smem<true, unsigned long long>());
+    cudaFuncSetAttribute(k_besc_rows<Shape, false, T, unsigned>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)Shape::template smem<false, unsigned>());
+}
+
+// Launch the CTA-per-row bitonic kernel of `Shape` on `s`: numeric keys pack the product
+// index below the column and need 64 bits when the two do not fit in 32.
+template <typename Shape, bool kNum, typename T>
+void launch_besc(const SpgemmArgs<T> &g, const int *list, const int *count_ptr, int *cursor, int grid,
+                 cudaStream_t s)
+{
+    if (!kNum) {
+        k_besc_rows<Shape, false, T, unsigned>
+            <<<grid, Shape::kThreads, Shape::template smem<false, unsigned>(), s>>>(g, list, count_ptr, cursor);
+    } else if (ceil_log2(std::max(g.N, 2)) + Shape::kIdBits <= 32) {
+        k_besc_rows<Shape, true, T, unsigned>
+            <<<grid, Shape::kThreads, Shape::template smem<true, unsigned>(), s>>>(g, list, count_ptr, cursor);
+    } else {
+        k_besc_rows<Shape, true, T, unsigned long long>
+            <<<grid, Shape::kThreads, Shape::template smem<true, unsigned long long>(), s>>>(g, list, count_ptr,
+                                                                                             cursor);
+    }
+}
+
 template <typename T>
 void set_smem_attrs()
 {
     cudaFuncSetAttribute(k_warp_rows<true, T, kWarpTableMax>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)warp_rows_smem<true, T, kWarpTableMax>());
-    cudaFuncSetAttribute(k_warp_rows<false, T, 2 * kEsc1FlopMax>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)warp_rows_smem<false, T, 2 * kEsc1FlopMax>());
     cudaFuncSetAttribute(k_warp_rows<true, T, 2 * kSplitNnz>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)warp_rows_smem<true, T, 2 * kSplitNnz>());
-    cudaFuncSetAttribute(k_esc_rows<EscSmall, true, T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)EscSmall::kNumericSmem);
     cudaFuncSetAttribute(k_esc_rows<EscLarge, true, T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)EscLarge::kNumericSmem);
-    cudaFuncSetAttribute(k_esc_rows<EscSmall, false, T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)EscSmall::kSymbolicSmem);
     cudaFuncSetAttribute(k_esc_rows<EscLarge, false, T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)EscLarge::kSymbolicSmem);
-    cudaFuncSetAttribute(k_esc_rows<EscMid, true, T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)EscMid::kNumericSmem);
     cudaFuncSetAttribute(k_esc_rows<EscMid, false, T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)EscMid::kSymbolicSmem);
+    cudaFuncSetAttribute(k_warp_rows<false, T, 2 * kEsc1FlopMax>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)warp_rows_smem<false, T, 2 * kEsc1FlopMax>());
+    set_besc_attrs<BescE1, T>();
+    set_besc_attrs<BescMid, T>();
     cudaFuncSetAttribute(k_wsort_rows<4, true, T, unsigned>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)WsortShape<4>::smem<true, T, unsigned>());
     cudaFuncSetAttribute(k_wsort_rows<4, true, T, unsigned long long>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -221,8 +247,8 @@ int launch_classes(ops_handle_s *h, const SpgemmArgs<T> &g, cudaStream_t st)
                 ++h->launches;
                 cudaStream_t sx = fork_x(0, s);
                 if (!sx) return fail(h, OPS_CUDA_ERROR, "stream fork failed");
-                k_esc_rows<EscSmall, true, T><<<std::min(n, sms * 8), EscSmall::kThreads, EscSmall::kNumericSmem, sx>>>(
-                    g, esc_list, &h->info->split[2], &h->info->next[1][c]);
+                launch_besc<BescE1, true, T>(g, esc_list, &h->info->split[2], &h->info->next[1][c],
+                                             std::min(n, sms * 8), sx);
                 OPS_CUDA(h, cudaGetLastError());
                 ++h->launches;
                 if (!join_x(0, s)) return fail(h, OPS_CUDA_ERROR, "stream join failed");
@@ -262,9 +288,11 @@ int launch_classes(ops_handle_s *h, const SpgemmArgs<T> &g, cudaStream_t st)
                     OPS_CUDA(h, cudaGetLastError());
                     ++h->launches;
                 }
-                const size_t lsmem = kNum ? EscLarge::kNumericSmem : EscLarge::kSymbolicSmem;
-                k_esc_rows<EscLarge, kNum, T><<<std::min(n, sms), EscLarge::kThreads, lsmem, sx>>>(
-                    g, large_list, &h->info->split2[1], &h->info->next[kNum][c]);
+                // large rows: radix-sort expand/sort/compress (for 8K-16K products the
+                // 3 radix passes beat a 16K-key bitonic network); counting by hash table
+                k_esc_rows<EscLarge, kNum, T>
+                    <<<std::min(n, sms), EscLarge::kThreads, kNum ? EscLarge::kNumericSmem : EscLarge::kSymbolicSmem,
+                       sx>>>(g, large_list, &h->info->split2[1], &h->info->next[kNum][c]);
                 OPS_CUDA(h, cudaGetLastError());
                 ++h->launches;
                 if (!join_x(1, s)) return fail(h, OPS_CUDA_ERROR, "stream join failed");
@@ -273,9 +301,13 @@ int launch_classes(ops_handle_s *h, const SpgemmArgs<T> &g, cudaStream_t st)
                     OPS_CUDA(h, cudaGetLastError());
                     ++h->launches;
                 }
-                const size_t msmem = kNum ? EscMid::kNumericSmem : EscMid::kSymbolicSmem;
-                k_esc_rows<EscMid, kNum, T><<<std::min(n, sms * 3), EscMid::kThreads, msmem, s>>>(
-                    g, mid_list, &h->info->split2[0], &h->info->next_mid[kNum]);
+                if (kNum) {  // mid rows: bitonic expand/sort/compress
+                    launch_besc<BescMid, true, T>(g, mid_list, &h->info->split2[0], &h->info->next_mid[1],
+                                                  std::min(n, sms * 4), s);
+                } else {  // counting by hash table
+                    k_esc_rows<EscMid, false, T><<<std::min(n, sms * 4), EscMid::kThreads, EscMid::kSymbolicSmem, s>>>(
+                        g, mid_list, &h->info->split2[0], &h->info->next_mid[0]);
+                }
                 break;
             }
             case kClsD: {

@@ -26,33 +26,53 @@ __device__ __forceinline__ int wpad(int e) { return e + (e >> 5); }
 
 // Ascending bitonic sort of the 32*PER keys held blocked across the warp.  Partner
 // distances of PER and above are exchanged with shuffles, smaller ones in registers.
+// The merge size k and the shuffle distances run as loops, not unrolled: only the
+// per-register work is unrolled, which keeps the code small enough for the instruction
+// cache (a fully unrolled 512-key network stalls on instruction fetch).
 template <int PER, typename KT>
 __device__ __forceinline__ void warp_bitonic_blocked(KT (&x)[PER])
 {
     const int lane = lane_id();
     constexpr int n = 32 * PER;
+    // merges of size <= PER are entirely in registers
 #pragma unroll
-    for (int k = 2; k <= n; k <<= 1) {
+    for (int k = 2; k <= PER; k <<= 1) {
 #pragma unroll
         for (int j = k >> 1; j > 0; j >>= 1) {
-            if (j >= PER) {
-                const bool lower = ((lane * PER) & j) == 0;
 #pragma unroll
-                for (int i = 0; i < PER; ++i) {
+            for (int i = 0; i < PER; ++i) {
+                if ((i & j) == 0) {
                     const bool asc = ((lane * PER + i) & k) == 0;
-                    const KT y = __shfl_xor_sync(kFull, x[i], j / PER);
-                    x[i] = (lower == asc) ? (x[i] < y ? x[i] : y) : (x[i] < y ? y : x[i]);
+                    const KT a = x[i], b = x[i | j];
+                    const bool sw = asc ? (b < a) : (a < b);
+                    x[i] = sw ? b : a;
+                    x[i | j] = sw ? a : b;
                 }
-            } else {
+            }
+        }
+    }
+#pragma unroll 1
+    for (int k = 2 * PER; k <= n; k <<= 1) {
+        // direction is uniform over a lane's registers: k > PER
+        const bool asc = ((lane * PER) & k) == 0;
+#pragma unroll 1
+        for (int j = k >> 1; j >= PER; j >>= 1) {
+            const bool take_min = (((lane * PER) & j) == 0) == asc;
 #pragma unroll
-                for (int i = 0; i < PER; ++i) {
-                    if ((i & j) == 0) {
-                        const bool asc = ((lane * PER + i) & k) == 0;
-                        const KT a = x[i], b = x[i | j];
-                        const bool sw = asc ? (b < a) : (a < b);
-                        x[i] = sw ? b : a;
-                        x[i | j] = sw ? a : b;
-                    }
+            for (int i = 0; i < PER; ++i) {
+                const KT y = __shfl_xor_sync(kFull, x[i], j / PER);
+                x[i] = take_min ? (x[i] < y ? x[i] : y) : (x[i] < y ? y : x[i]);
+            }
+        }
+#pragma unroll
+        for (int j = PER / 2; j > 0; j >>= 1) {
+#pragma unroll
+            for (int i = 0; i < PER; ++i) {
+                if ((i & j) == 0) {
+                    const KT a = x[i], b = x[i | j];
+                    const bool sw = asc ? (b < a) : (a < b);
+                    x[i] = sw ? b : a;
+                    x[i | j] = sw ? a : b;
                 }
             }
         }
@@ -64,7 +84,8 @@ struct WsortShape {
     static constexpr int kMax = 32 * PMAX;                     // products per row, at most
     static constexpr int kWarps = PMAX <= 4 ? 8 : 4;           // warps per CTA
     static constexpr int kThreads = 32 * kWarps;
-    static constexpr int kIdBits = PMAX <= 4 ? 7 : (PMAX <= 8 ? 8 : 9);
+    static constexpr int kMinBlocks = PMAX >= 32 ? 4 : 1;      // caps the 32-key variant at 128 registers
+    static constexpr int kIdBits = PMAX <= 4 ? 7 : (PMAX <= 8 ? 8 : (PMAX <= 16 ? 9 : 10));
     static constexpr int kKeySlots = kMax + kMax / 32;         // padded key array
     static constexpr int kHeadSlots = kMax + 32;               // run heads + end marker
 
@@ -145,10 +166,11 @@ __device__ __forceinline__ int wsort_row(const SpgemmArgs<T> &g, int flop, KT *s
 }
 
 // One warp per listed row (flop <= 32*PMAX).  Rows of at most 128 products sort 128 keys,
-// at most 256 sort 256, the rest 512 (PMAX = 16 only).  The row count is read from
+// at most 256 sort 256, and so on up to 32*PMAX (PMAX = 32 is used for the symbolic
+// count of rows of up to 1024 products).  The row count is read from
 // device memory, so lists split on the device need no host round trip.
 template <int PMAX, bool kNum, typename T, typename KT>
-__global__ void __launch_bounds__(WsortShape<PMAX>::kThreads) k_wsort_rows(SpgemmArgs<T> g, const int *__restrict__ list,
+__global__ void __launch_bounds__(WsortShape<PMAX>::kThreads, WsortShape<PMAX>::kMinBlocks) k_wsort_rows(SpgemmArgs<T> g, const int *__restrict__ list,
                                                                          const int *count_ptr)
 {
     using Sh = WsortShape<PMAX>;
@@ -244,16 +266,21 @@ __global__ void __launch_bounds__(WsortShape<PMAX>::kThreads) k_wsort_rows(Spgem
         }
         if (bad) atomicOr(&g.info->flags, kErrBadColumn);
         __syncwarp();
-        int total;
+        // the smallest power-of-two network that holds the row (rows are listed here
+        // only if flop <= 32*PMAX)
+        int total = 0;
         if (flop <= 128) {
             total = wsort_row<4, kIdBits, kNum, T, KT>(g, flop, skey, heads, sa, sb, off, n_expect);
         } else if constexpr (PMAX >= 8) {
-            if (flop <= 256)
+            if (flop <= 256) {
                 total = wsort_row<8, kIdBits, kNum, T, KT>(g, flop, skey, heads, sa, sb, off, n_expect);
-            else
-                total = wsort_row<PMAX, kIdBits, kNum, T, KT>(g, flop, skey, heads, sa, sb, off, n_expect);
-        } else {
-            total = 0;  // not reached: rows are listed here only if flop <= 32*PMAX
+            } else if constexpr (PMAX >= 16) {
+                if (flop <= 512) {
+                    total = wsort_row<16, kIdBits, kNum, T, KT>(g, flop, skey, heads, sa, sb, off, n_expect);
+                } else if constexpr (PMAX >= 32) {
+                    total = wsort_row<32, kIdBits, kNum, T, KT>(g, flop, skey, heads, sa, sb, off, n_expect);
+                }
+            }
         }
         if constexpr (!kNum) {
             if (lane == 0) {
@@ -265,7 +292,7 @@ __global__ void __launch_bounds__(WsortShape<PMAX>::kThreads) k_wsort_rows(Spgem
         }
         __syncwarp();
     }
-    if constexpr (!kNum) block_add_u64(nnz_acc, &g.info->total_nnz);
+    if constexpr (!kNum) warp_add_u64(nnz_acc, &g.info->total_nnz);
 }
 
 }  // namespace opsg
