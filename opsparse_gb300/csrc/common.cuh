@@ -210,15 +210,70 @@ __device__ __forceinline__ void warp_products(int a_begin, int a_end, int stride
     }
 }
 
-// Row-aligned enumeration for rows whose B rows are long: the warp loads 32 A entries at
-// a time, then walks them in order with the lanes spread over one B row per step
-// (several steps for B rows longer than 32).  A B row's columns are distinct, so the
-// lanes of a step never share a key: no de-duplication is needed, and successive steps
-// (ascending j) are separated by the caller's __syncwarp.  f(valid, k, a) is called once
-// per step with all lanes converged.
-template <bool kNeedVal, typename T, typename F>
-__device__ __forceinline__ void warp_rowwise_products(int a_begin, int a_end, const int *__restrict__ acol,
-                                                      const T *__restrict__ aval, const int *__restrict__ brpt, F &&f)
+// Ascending bitonic sort of the 32*PER keys held blocked across the warp.  Partner
+// distances of PER and above are exchanged with shuffles, smaller ones in registers.
+// The merge size k and the shuffle distances run as loops, not unrolled: only the
+// per-register work is unrolled, which keeps the code small enough for the instruction
+// cache (a fully unrolled 512-key network stalls on instruction fetch).
+template <int PER, typename KT>
+__device__ __forceinline__ void warp_bitonic_blocked(KT (&x)[PER])
+{
+    const int lane = lane_id();
+    constexpr int n = 32 * PER;
+    // merges of size <= PER are entirely in registers
+#pragma unroll
+    for (int k = 2; k <= PER; k <<= 1) {
+#pragma unroll
+        for (int j = k >> 1; j > 0; j >>= 1) {
+#pragma unroll
+            for (int i = 0; i < PER; ++i) {
+                if ((i & j) == 0) {
+                    const bool asc = ((lane * PER + i) & k) == 0;
+                    const KT a = x[i], b = x[i | j];
+                    const bool sw = asc ? (b < a) : (a < b);
+                    x[i] = sw ? b : a;
+                    x[i | j] = sw ? a : b;
+                }
+            }
+        }
+    }
+#pragma unroll 1
+    for (int k = 2 * PER; k <= n; k <<= 1) {
+        // direction is uniform over a lane's registers: k > PER
+        const bool asc = ((lane * PER) & k) == 0;
+#pragma unroll 1
+        for (int j = k >> 1; j >= PER; j >>= 1) {
+            const bool take_min = (((lane * PER) & j) == 0) == asc;
+#pragma unroll
+            for (int i = 0; i < PER; ++i) {
+                const KT y = __shfl_xor_sync(kFull, x[i], j / PER);
+                x[i] = take_min ? (x[i] < y ? x[i] : y) : (x[i] < y ? y : x[i]);
+            }
+        }
+#pragma unroll
+        for (int j = PER / 2; j > 0; j >>= 1) {
+#pragma unroll
+            for (int i = 0; i < PER; ++i) {
+                if ((i & j) == 0) {
+                    const KT a = x[i], b = x[i | j];
+                    const bool sw = asc ? (b < a) : (a < b);
+                    x[i] = sw ? b : a;
+                    x[i | j] = sw ? a : b;
+                }
+            }
+        }
+    }
+}
+
+// Row-aligned enumeration with the operands loaded ahead: the first 32 entries of kU
+// consecutive B rows are loaded together, then handed to f in order (B rows longer than
+// 32 continue chunk by chunk before the next row starts).  f(valid, col, b, a) is called
+// with all lanes converged, in ascending j and, within a B row, ascending position.
+template <int kU, bool kNeedVal, typename T, typename F>
+__device__ __forceinline__ void warp_rowwise_products_pf(int a_begin, int a_end, const int *__restrict__ acol,
+                                                         const T *__restrict__ aval, const int *__restrict__ brpt,
+                                                         const int *__restrict__ bcol, const T *__restrict__ bval,
+                                                         F &&f)
 {
     const int lane = lane_id();
     for (int wa = a_begin; wa < a_end; wa += 32) {
@@ -232,11 +287,31 @@ __device__ __forceinline__ void warp_rowwise_products(int a_begin, int a_end, co
             if (kNeedVal) av = __ldg(aval + q);
         }
         const int m = min(32, a_end - wa);
-        for (int t = 0; t < m; ++t) {
-            const int s0 = __shfl_sync(kFull, b0, t);
-            const int s1 = __shfl_sync(kFull, b1, t);
-            const T a = kNeedVal ? shfl(av, t) : T(0);
-            for (int c = s0; c < s1; c += 32) f(c + lane < s1, c + lane, a);
+        for (int t0 = 0; t0 < m; t0 += kU) {
+            int col[kU], s0[kU], s1[kU];
+            T bv[kU], a[kU];
+            bool v[kU];
+#pragma unroll
+            for (int u = 0; u < kU; ++u) {
+                const int t = min(t0 + u, 31);
+                s0[u] = __shfl_sync(kFull, b0, t);
+                s1[u] = __shfl_sync(kFull, b1, t);
+                a[u] = kNeedVal ? shfl(av, t) : T(0);
+                v[u] = t0 + u < m && s0[u] + lane < s1[u];
+                col[u] = v[u] ? __ldg(bcol + s0[u] + lane) : 0;
+                bv[u] = (kNeedVal && v[u]) ? __ldg(bval + s0[u] + lane) : T(0);
+            }
+#pragma unroll
+            for (int u = 0; u < kU; ++u) {
+                if (t0 + u >= m) break;  // warp-uniform
+                f(v[u], col[u], bv[u], a[u]);
+                for (int c = s0[u] + 32; c < s1[u]; c += 32) {
+                    const bool vv = c + lane < s1[u];
+                    const int cc = vv ? __ldg(bcol + c + lane) : 0;
+                    const T bb = (kNeedVal && vv) ? __ldg(bval + c + lane) : T(0);
+                    f(vv, cc, bb, a[u]);
+                }
+            }
         }
     }
 }

@@ -468,6 +468,30 @@ __global__ void __launch_bounds__(256) k_reg_rows(SpgemmArgs<T> g, const int *__
 // contributions in ascending j.  Numeric then compacts the table and places each entry
 // at its rank among the row's columns.
 // ==================================================================================
+// Writes the n compacted (column, value) entries of a warp-hash row to C in column order:
+// keys (column << 8 | slot) are sorted in registers by the warp bitonic network.
+template <int PER, typename T>
+__device__ __forceinline__ void warp_table_sort_write(const SpgemmArgs<T> &g, const int *keys,
+                                                      const typename Acc<T>::S *vals, int n, int off)
+{
+    const int lane = lane_id();
+    unsigned long long x[PER];
+#pragma unroll
+    for (int i = 0; i < PER; ++i) {
+        const int e = i * 32 + lane;  // any arrangement will do: the network sorts it
+        x[i] = e < n ? (((unsigned long long)(unsigned)keys[e] << 8) | (unsigned)e) : ~0ull;
+    }
+    warp_bitonic_blocked<PER, unsigned long long>(x);
+#pragma unroll
+    for (int i = 0; i < PER; ++i) {
+        const int e = lane * PER + i;
+        if (e < n) {
+            g.c_col[off + e] = (int)(x[i] >> 8);
+            g.c_val[off + e] = Acc<T>::fin(vals[x[i] & 255u]);
+        }
+    }
+}
+
 constexpr int kWarpRowsThreads = 256;
 constexpr int kCountUnroll = 4;  // symbolic: chunks whose column loads are issued together
 
@@ -558,19 +582,21 @@ __global__ void __launch_bounds__(kWarpRowsThreads) k_warp_rows(SpgemmArgs<T> g,
                 }
             }
         } else if (row_products >= 16 * (a1 - a0)) {
-            // long B rows: one B row per step, every lane owns a distinct key
-            warp_rowwise_products<kNum, T>(a0, a1, g.acol, g.aval, g.brpt, [&](bool valid, int k, T av) {
-                if (valid) {
-                    const int col = __ldg(g.bcol + k);
-                    bool is_new = false;
-                    const int slot = table_claim(keys, col, log_ts, &is_new, &g.info->flags);
-                    cnt += is_new ? 1 : 0;
-                    if constexpr (kNum) {
-                        if (slot >= 0) vals[slot] = AccT::step(vals[slot], av, __ldg(g.bval + k));
-                    }
-                }
-                __syncwarp();
-            });
+            // long B rows: one B row per step, every lane owns a distinct key; four
+            // B rows' operands are loaded ahead of their steps
+            warp_rowwise_products_pf<4, kNum, T>(a0, a1, g.acol, g.aval, g.brpt, g.bcol, g.bval,
+                                                 [&](bool valid, int col, T bv, T av) {
+                                                     if (valid) {
+                                                         bool is_new = false;
+                                                         const int slot =
+                                                             table_claim(keys, col, log_ts, &is_new, &g.info->flags);
+                                                         cnt += is_new ? 1 : 0;
+                                                         if constexpr (kNum) {
+                                                             if (slot >= 0) vals[slot] = AccT::step(vals[slot], av, bv);
+                                                         }
+                                                     }
+                                                     __syncwarp();
+                                                 });
         } else
         warp_products<kNum, T>(a0, a1, 32, g.acol, g.aval, g.brpt, [&](bool valid, int k, T av, int) {
             const int col = valid ? __ldg(g.bcol + k) : kEmpty;
@@ -623,33 +649,12 @@ __global__ void __launch_bounds__(kWarpRowsThreads) k_warp_rows(SpgemmArgs<T> g,
                     g.c_col[off + rank] = ke;
                     g.c_val[off + rank] = AccT::fin(vals[e]);
                 }
-            } else {  // bitonic sort of the compacted entries, padded with INT_MAX keys
-                int m = 64;
-                while (m < nw) m <<= 1;  // m <= ts: the table holds at least 2*n slots
-                for (int i = nw + lane; i < m; i += 32) keys[i] = INT_MAX;
-                __syncwarp();
-                for (int k2 = 2; k2 <= m; k2 <<= 1) {
-                    for (int j2 = k2 >> 1; j2 > 0; j2 >>= 1) {
-                        for (int i = lane; i < m; i += 32) {
-                            const int ixj = i ^ j2;
-                            if (ixj > i) {
-                                const int ki = keys[i], kx = keys[ixj];
-                                if ((ki > kx) == ((i & k2) == 0)) {
-                                    keys[i] = kx;
-                                    keys[ixj] = ki;
-                                    const S tv = vals[i];
-                                    vals[i] = vals[ixj];
-                                    vals[ixj] = tv;
-                                }
-                            }
-                        }
-                        __syncwarp();
-                    }
-                }
-                for (int e = lane; e < nw; e += 32) {
-                    g.c_col[off + e] = keys[e];
-                    g.c_val[off + e] = AccT::fin(vals[e]);
-                }
+            } else if (nw <= 128) {
+                warp_table_sort_write<4, T>(g, keys, vals, nw, off);
+            } else if (nw <= 256) {
+                warp_table_sort_write<8, T>(g, keys, vals, nw, off);
+            } else {  // not reached: numeric rows here have at most TMAX/2 outputs
+                if (lane == 0) atomicOr(&g.info->flags, kErrCountMismatch);
             }
             __syncwarp();
         }

@@ -24,61 +24,6 @@ constexpr int kWsortFlopMax = 512;  // largest row of the 16-per-lane variant
 // conflicts, and so does the expansion's contiguous stores.
 __device__ __forceinline__ int wpad(int e) { return e + (e >> 5); }
 
-// Ascending bitonic sort of the 32*PER keys held blocked across the warp.  Partner
-// distances of PER and above are exchanged with shuffles, smaller ones in registers.
-// The merge size k and the shuffle distances run as loops, not unrolled: only the
-// per-register work is unrolled, which keeps the code small enough for the instruction
-// cache (a fully unrolled 512-key network stalls on instruction fetch).
-template <int PER, typename KT>
-__device__ __forceinline__ void warp_bitonic_blocked(KT (&x)[PER])
-{
-    const int lane = lane_id();
-    constexpr int n = 32 * PER;
-    // merges of size <= PER are entirely in registers
-#pragma unroll
-    for (int k = 2; k <= PER; k <<= 1) {
-#pragma unroll
-        for (int j = k >> 1; j > 0; j >>= 1) {
-#pragma unroll
-            for (int i = 0; i < PER; ++i) {
-                if ((i & j) == 0) {
-                    const bool asc = ((lane * PER + i) & k) == 0;
-                    const KT a = x[i], b = x[i | j];
-                    const bool sw = asc ? (b < a) : (a < b);
-                    x[i] = sw ? b : a;
-                    x[i | j] = sw ? a : b;
-                }
-            }
-        }
-    }
-#pragma unroll 1
-    for (int k = 2 * PER; k <= n; k <<= 1) {
-        // direction is uniform over a lane's registers: k > PER
-        const bool asc = ((lane * PER) & k) == 0;
-#pragma unroll 1
-        for (int j = k >> 1; j >= PER; j >>= 1) {
-            const bool take_min = (((lane * PER) & j) == 0) == asc;
-#pragma unroll
-            for (int i = 0; i < PER; ++i) {
-                const KT y = __shfl_xor_sync(kFull, x[i], j / PER);
-                x[i] = take_min ? (x[i] < y ? x[i] : y) : (x[i] < y ? y : x[i]);
-            }
-        }
-#pragma unroll
-        for (int j = PER / 2; j > 0; j >>= 1) {
-#pragma unroll
-            for (int i = 0; i < PER; ++i) {
-                if ((i & j) == 0) {
-                    const KT a = x[i], b = x[i | j];
-                    const bool sw = asc ? (b < a) : (a < b);
-                    x[i] = sw ? b : a;
-                    x[i | j] = sw ? a : b;
-                }
-            }
-        }
-    }
-}
-
 template <int PMAX>
 struct WsortShape {
     static constexpr int kMax = 32 * PMAX;                     // products per row, at most
