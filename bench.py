@@ -226,6 +226,7 @@ def run_ours(args, desc, dt, data, n, rank, world, local_rank):
     out = step()
     nnz_c = out[3]
     phases = h.timings()
+    subclass = h.subclass_rows()
     release(out)
     h.set_timing(0)
     P = int(phases["flop"])
@@ -316,6 +317,7 @@ def run_ours(args, desc, dt, data, n, rank, world, local_rank):
                                                              "numeric", "total")},
         "kernels_ms": per_kernel,
         "class_rows": dict(zip(names, phases["class_rows"])),
+        "subclass_rows": subclass,
         "e2e": {"value": e2e_gf, "unit": "GFLOPS", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "ms_per_step": e2e_t},
         "gpu_launches": launches,

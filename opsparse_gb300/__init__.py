@@ -126,10 +126,10 @@ class Handle:
 
     def subclass_rows(self) -> dict:
         """Rows per sub-kernel of the last call: E1 numeric (warp sort, warp hash,
-        expand/sort/compress) and E2 (mid, large shape)."""
-        arr = (C.c_int32 * 5)()
-        check(self.lib.ops_handle_subclass_rows(self.h, arr, 5), self.h)
-        return dict(zip(("e1_sort", "e1_hash", "e1_esc", "e2_mid", "e2_large"), list(arr)))
+        expand/sort/compress), E2 (mid, large shape) and D (whole-GPU sort, dense kernel)."""
+        arr = (C.c_int32 * 7)()
+        check(self.lib.ops_handle_subclass_rows(self.h, arr, 7), self.h)
+        return dict(zip(("e1_sort", "e1_hash", "e1_esc", "e2_mid", "e2_large", "d_sort", "d_dense"), list(arr)))
 
     # -- two-phase ------------------------------------------------------------
     def symbolic(self, A: CsrMatrix, B: CsrMatrix, c_rpt=None, stream=None):

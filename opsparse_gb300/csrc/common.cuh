@@ -71,6 +71,28 @@ struct DevInfo {
     int split[3];                 // E1 rows re-binned for the numeric phase: [warp sort, hash, expand/sort]
     int split2[2];                // E2 rows by size, fixed at the symbolic phase: [mid shape, large shape]
     int next_mid[2];              // row cursor of the mid-shape E2 kernel [symbolic, numeric]
+    unsigned long long d_len_a;   // A entries of the D rows
+    unsigned long long d_flop;    // products of the D rows
+    int d_cursor;                 // output cursor of the D-row expansion
+};
+
+// Arguments shared by every SpGEMM kernel.
+template <typename T>
+struct SpgemmArgs {
+    const int *__restrict__ arpt;
+    const int *__restrict__ acol;
+    const T *__restrict__ aval;
+    const int *__restrict__ brpt;
+    const int *__restrict__ bcol;
+    const T *__restrict__ bval;
+    int M;             // rows of A and C
+    int K;             // cols of A == rows of B
+    int N;             // cols of B and C
+    const int *__restrict__ row_flop;
+    int *c_rpt;        // symbolic: per-row nnz written at [r]; numeric: row offsets
+    int *c_col;
+    T *c_val;
+    DevInfo *info;
 };
 
 __device__ __forceinline__ int lane_id() { return threadIdx.x & 31; }
@@ -80,6 +102,14 @@ __device__ __forceinline__ unsigned lanemask_lt()
     unsigned m;
     asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
     return m;
+}
+
+// 64-bit warp sum.
+__device__ __forceinline__ unsigned long long warp_sum_u64(unsigned long long v)
+{
+#pragma unroll
+    for (int d = 16; d >= 1; d >>= 1) v += __shfl_xor_sync(kFull, v, d);
+    return v;
 }
 
 // Fibonacci hashing: the top log2(TS) bits of key * 2^32/phi.

@@ -74,6 +74,9 @@ struct ops_handle_s {
     int counts[kNumClasses] = {};
     long long plan_flop = 0;
     long long plan_nnz = 0;
+    int d_rows_path[2] = {};      // D rows of the last phase by [whole-GPU sort, dense kernel]
+    long long plan_d_flop = 0;    // products of the D rows
+    long long plan_d_len_a = 0;   // A entries of the D rows
 
     size_t map_budget = size_t(8) << 30;  // largest product map the backward may keep
     opsg::Thresholds th = opsg::default_thresholds();
@@ -84,6 +87,13 @@ struct ops_handle_s {
 };
 
 namespace opsg_internal {
+
+// D rows (more than the E2 capacity) by whole-GPU expand / stable radix sort / compress
+// (gesc.cu).  Returns OPS_NOT_SUPPORTED, having launched nothing, when the products do
+// not fit 32-bit positions or the scratch exceeds the handle's dense budget; the caller
+// then uses the dense-row kernel.
+template <typename T>
+int run_d_rows(ops_handle_s *h, const opsg::SpgemmArgs<T> &g, const int *list, int n, bool numeric, cudaStream_t s);
 
 inline int status_of(cudaError_t e) { return e == cudaErrorMemoryAllocation ? OPS_OOM : OPS_CUDA_ERROR; }
 

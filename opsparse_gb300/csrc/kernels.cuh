@@ -27,32 +27,6 @@
 
 namespace opsg {
 
-template <typename T>
-struct SpgemmArgs {
-    const int *__restrict__ arpt;
-    const int *__restrict__ acol;
-    const T *__restrict__ aval;
-    const int *__restrict__ brpt;
-    const int *__restrict__ bcol;
-    const T *__restrict__ bval;
-    int M;             // rows of A and C
-    int K;             // cols of A == rows of B
-    int N;             // cols of B and C
-    const int *__restrict__ row_flop;
-    int *c_rpt;        // symbolic: per-row nnz written at [r]; numeric: row offsets
-    int *c_col;
-    T *c_val;
-    DevInfo *info;
-};
-
-// 64-bit warp sum.
-__device__ __forceinline__ unsigned long long warp_sum_u64(unsigned long long v)
-{
-#pragma unroll
-    for (int d = 16; d >= 1; d >>= 1) v += __shfl_xor_sync(kFull, v, d);
-    return v;
-}
-
 // Sum of one u64 per thread over the warp, added to *dst by lane 0: no block barrier,
 // so warps of one CTA that finish early do not wait for the others.
 __device__ __forceinline__ void warp_add_u64(unsigned long long v, unsigned long long *dst)
@@ -221,6 +195,8 @@ static __global__ void __launch_bounds__(kSetupThreads) k_setup(const int *__res
             cls = kClsE2;
         } else {
             cls = kClsD;
+            atomicAdd(&info->d_len_a, (unsigned long long)lenA);
+            atomicAdd(&info->d_flop, (unsigned long long)flop);
         }
     }
 

@@ -311,8 +311,18 @@ int launch_classes(ops_handle_s *h, const SpgemmArgs<T> &g, cudaStream_t st)
                 break;
             }
             case kClsD: {
-                k_dense_rows<kNum, T><<<std::min(n, h->dense_ctas), kDenseRowsThreads, 0, s>>>(
-                    g, list, n, dense_view<T>(h, g.N));
+                // whole-GPU expand/sort/compress; the CTA-per-row dense kernel when the
+                // packed keys or the scratch do not fit
+                const int st_d = run_d_rows<T>(h, g, list, n, kNum, s);
+                h->d_rows_path[0] = st_d == OPS_OK ? n : 0;
+                h->d_rows_path[1] = st_d == OPS_NOT_SUPPORTED ? n : 0;
+                if (st_d == OPS_NOT_SUPPORTED) {
+                    OPS_CHECK(ensure_dense(h, g.N, n, s));
+                    k_dense_rows<kNum, T><<<std::min(n, h->dense_ctas), kDenseRowsThreads, 0, s>>>(
+                        g, list, n, dense_view<T>(h, g.N));
+                } else if (st_d != OPS_OK) {
+                    return st_d;
+                }
                 break;
             }
         }
@@ -377,7 +387,8 @@ int run_symbolic(ops_handle_s *h, const Mat &A, const Mat &B, int *c_rpt, long l
     h->plan_K = A.cols;
     h->plan_N = B.cols;
     h->plan_flop = (long long)hi.total_flop;
-    if (h->counts[kClsD] > 0) OPS_CHECK(ensure_dense(h, B.cols, h->counts[kClsD], st));
+    h->plan_d_flop = (long long)hi.d_flop;
+    h->plan_d_len_a = (long long)hi.d_len_a;
 
     SpgemmArgs<double> g{};
     g.arpt = A.rpt;
@@ -417,7 +428,6 @@ int run_numeric(ops_handle_s *h, const Mat &A, const Mat &B, const int *c_rpt, i
     if (!h->plan_valid || h->plan_M != A.rows || h->plan_K != A.cols || h->plan_N != B.cols ||
         h->plan_arpt != A.rpt || h->plan_acol != A.col || h->plan_brpt != B.rpt || h->plan_bcol != B.col)
         return fail(h, OPS_NOT_SUPPORTED, "numeric phase without a matching symbolic phase on this handle");
-    if (h->counts[kClsD] > 0) OPS_CHECK(ensure_dense(h, B.cols, h->counts[kClsD], st));
     OPS_CUDA(h, cudaMemsetAsync(&h->info->flags, 0, sizeof(int), st));
     OPS_CUDA(h, cudaMemsetAsync(h->info->next[1], 0, sizeof(h->info->next[1]), st));
     OPS_CUDA(h, cudaMemsetAsync(h->info->split, 0, sizeof(h->info->split), st));
@@ -654,7 +664,9 @@ const char *ops_handle_last_error(ops_handle_t h) { return h ? h->last_error.c_s
 int ops_handle_subclass_rows(ops_handle_t h, int32_t *out, int n)
 {
     if (!h || !out || n < 0) return OPS_INVALID_ARGUMENT;
-    int v[5] = {};
+    int v[7] = {};
+    v[5] = h->d_rows_path[0];
+    v[6] = h->d_rows_path[1];
     if (h->info) {
         DevInfo d{};
         OPS_CUDA(h, cudaMemcpy(&d, h->info, sizeof(DevInfo), cudaMemcpyDeviceToHost));
@@ -664,7 +676,7 @@ int ops_handle_subclass_rows(ops_handle_t h, int32_t *out, int n)
         v[3] = d.split2[0];
         v[4] = d.split2[1];
     }
-    for (int i = 0; i < n && i < 5; ++i) out[i] = v[i];
+    for (int i = 0; i < n && i < 7; ++i) out[i] = v[i];
     return OPS_OK;
 }
 

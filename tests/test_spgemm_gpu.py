@@ -95,7 +95,33 @@ def test_subclass_coverage(cuda, handle):
         run_case(cuda, handle, case, cuda.float64)
         for k, v in handle.subclass_rows().items():
             seen[k] = seen.get(k, 0) + v
-    assert all(v > 0 for v in seen.values()), seen
+    assert all(v > 0 for k, v in seen.items() if k != "d_dense"), seen
+
+
+@pytest.mark.parametrize("dtype", ["f64", "f32"])
+def test_d_rows_dense_fallback(cuda, dtype):
+    """With a scratch budget too small for the whole-GPU sort, the D rows take the
+    CTA-per-row dense kernel; both give the oracle's bits."""
+    case = next(c for c in CASES if c[0] == "dense_row")
+    name, a, b, ncols = case
+    for budget, path in ((None, "d_sort"), (1 << 20, "d_dense")):
+        h = ops.Handle()
+        if budget:
+            h.set_dense_budget(budget)
+        if dtype == "f64":
+            rpt, col, val = run_case(cuda, h, case, cuda.float64)
+            orpt, ocol, oval = oracle.spgemm(*a, *b, ncols)
+            assert np.array_equal(val.view(np.uint64), oval.view(np.uint64)), path
+        else:
+            a32 = (a[0], a[1], a[2].astype(np.float32))
+            b32 = (b[0], b[1], b[2].astype(np.float32))
+            rpt, col, val = run_case(cuda, h, (name, a32, b32, ncols), cuda.float32)
+            orpt, ocol, oval = oracle.spgemm(*a32, *b32, ncols, dtype=np.float32)
+            assert np.array_equal(val.view(np.uint32), oval.view(np.uint32)), path
+        assert np.array_equal(rpt.astype(np.int64), orpt) and np.array_equal(col, ocol), path
+        sub = h.subclass_rows()
+        assert sub[path] > 0, (path, sub)
+        h.close()
 
 
 def _stretch_columns(case, factor=600):
@@ -128,6 +154,25 @@ def test_wide_columns(cuda, handle, dtype):
     assert np.array_equal(rpt.astype(np.int64), orpt)
     assert np.array_equal(col, f(ocol))
     assert handle.subclass_rows()["e1_sort"] > 0
+
+
+def test_many_d_rows_wide(cuda, handle):
+    """1,100 rows of 20,000 products each (D rows) over 11M columns: the D-row sort key
+    (row, column) needs more than 32 bits.  Results are the oracle's under the column map."""
+    rng = np.random.default_rng(21)
+    import scipy.sparse as sp
+    n = 20000
+    A = sp.random(1100, n, density=200 / n, random_state=rng, format="csr")
+    B = sp.random(n, n, density=100 / n, random_state=rng, format="csr")
+    from tests.cases import _csr
+    base = ("many_d", _csr(A), _csr(B), n)
+    case, f = _stretch_columns(base, factor=550)
+    rpt, col, val = run_case(cuda, handle, case, cuda.float64)
+    orpt, ocol, oval = oracle.spgemm(*base[1], *base[2], n)
+    assert np.array_equal(rpt.astype(np.int64), orpt)
+    assert np.array_equal(col, f(ocol))
+    assert np.array_equal(val.view(np.uint64), oval.view(np.uint64))
+    assert handle.subclass_rows()["d_sort"] > 1024
 
 
 def test_repeat_and_resize(cuda, handle):
