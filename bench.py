@@ -77,6 +77,15 @@ def bytes_alg(M, K, nnz_a, nnz_b, nnz_c, s):
     return sym + num
 
 
+def measured_traffic(workload):
+    """DRAM bytes per step of a workload, from the committed ncu launch-list summary."""
+    p = ROOT / "profiles" / "traffic.json"
+    if not p.exists():
+        return None, None
+    t = json.loads(p.read_text()).get(workload)
+    return (t["dram_bytes_per_step"], t["source"]) if t else (None, None)
+
+
 def measured_peak():
     p = ROOT / "MEASURED_PEAKS.json"
     if p.exists():
@@ -300,6 +309,7 @@ def run_ours(args, desc, dt, data, n, rank, world, local_rank):
     nnz_a = len(col)
     balg = bytes_alg(n, n, nnz_a, len(bcol), nnz_c, s)
     achieved = balg / (t_ms * 1e-3) / 1e9
+    traffic, traffic_src = measured_traffic(f'{desc["workload"]}/{dt}')
     kms = phases["kernel_ms"]
     names = ["R8", "R16", "R32", "W", "E1", "E2", "D"]
     per_kernel = {f"{ph}_{names[c]}": round(kms[i][c], 4) for i, ph in enumerate(("symbolic", "numeric"))
@@ -311,7 +321,8 @@ def run_ours(args, desc, dt, data, n, rank, world, local_rank):
         "config": dict(desc, l2="flushed between steps (256 MiB write outside the timed events)",
                        products=P, nnz_a=nnz_a, nnz_c=nnz_c, parallelism=f"replica x{world}"),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": None, "kernel": "whole SpGEMM pipeline (all launches of one C=A*B)",
+                     "traffic": traffic, "traffic_source": traffic_src,
+                     "kernel": "whole SpGEMM pipeline (all launches of one C=A*B); achieved and traffic per step",
                      "algorithmic_bytes": balg, "peak_kind": peak_kind},
         "phases_ms": {k: round(phases[k] * 1e3, 4) for k in ("symbolic_binning", "symbolic", "prefix", "allocate",
                                                              "numeric", "total")},

@@ -14,8 +14,10 @@
 //   4. Symbolic: count the run heads of each row.  Numeric: number the heads (scan),
 //      record where each run starts, and fold each run with one FMA per product — by
 //      one thread for runs of at most 32 products, by a warp for longer runs (the lanes
-//      gather the next 32 operands while lane 0 folds the current 32 from shared
-//      memory; a run is a chain of dependent FMAs and cannot be split).  C entry h of
+//      gather the operands of the next two batches of 32 while lane 0 folds the current
+//      32 from shared memory; a run is a chain of dependent FMAs and cannot be split, and
+//      a dependent FP64 FMA costs about 64 cycles on GB300, so the longest run bounds
+//      the phase).  C entry h of
 //      D row d goes to row_ptr[row] + h - (heads of the earlier D rows).
 #include <cub/cub.cuh>
 
@@ -263,8 +265,8 @@ __global__ void __launch_bounds__(kThreads) k_d_fold_short(const KT *__restrict_
     }
 }
 
-// Numeric, long runs: one warp per run.  The lanes gather the operands of the next 32
-// products while lane 0 folds the current 32 from shared memory, in order.
+// Numeric, long runs: one warp per run.  The lanes gather the operands of the next two
+// batches of 32 products while lane 0 folds the current 32 from shared memory, in order.
 template <typename T, typename KT>
 __global__ void __launch_bounds__(kThreads) k_d_fold_long(const KT *__restrict__ keys,
                                                           const unsigned long long *__restrict__ vals,
@@ -296,18 +298,34 @@ __global__ void __launch_bounds__(kThreads) k_d_fold_long(const KT *__restrict__
                 b = __ldg(bval + (int)(v & 0xffffffffu));
             }
         };
-        T na, nb;
+        // two batches in flight ahead of the fold: a batch's gather (two dependent loads)
+        // takes about as long as 32 dependent FP64 FMAs (~64 cycles each on this GPU)
+        T na, nb, na2, nb2;
         gather(t0 + lane, na, nb);
+        gather(t0 + 32 + lane, na2, nb2);
         typename AccT::S s = AccT::zero();
         int buf = 0;
         for (unsigned q = t0; q < t1; q += 32) {
             s_a[warp][buf][lane] = na;
             s_b[warp][buf][lane] = nb;
             __syncwarp();
-            gather(q + 32 + lane, na, nb);  // next batch in flight during the fold
+            na = na2;
+            nb = nb2;
+            gather(q + 64 + lane, na2, nb2);
             if (lane == 0) {
                 const int m = (int)min(32u, t1 - q);
-                for (int u = 0; u < m; ++u) s = AccT::step(s, s_a[warp][buf][u], s_b[warp][buf][u]);
+                if (m == 32) {  // operands to registers first: the chain waits only on the FMAs
+                    T ra[32], rb[32];
+#pragma unroll
+                    for (int u = 0; u < 32; ++u) {
+                        ra[u] = s_a[warp][buf][u];
+                        rb[u] = s_b[warp][buf][u];
+                    }
+#pragma unroll
+                    for (int u = 0; u < 32; ++u) s = AccT::step(s, ra[u], rb[u]);
+                } else {
+                    for (int u = 0; u < m; ++u) s = AccT::step(s, s_a[warp][buf][u], s_b[warp][buf][u]);
+                }
             }
             buf ^= 1;
         }
