@@ -117,39 +117,128 @@ __global__ void __launch_bounds__(256) k_build_pmap(const int *__restrict__ arpt
     }
 }
 
-// dA: one warp per row of A, lanes over the row's entries, each folding its B row in order.
+// The position in C of product (row i, B entry q) of A entry p: from the map, or by a
+// binary search of C's row i.
+template <bool kMap>
+__device__ __forceinline__ int prod_pos(const int *__restrict__ pmap, long long base, int t,
+                                        const int *__restrict__ c_rpt, const int *__restrict__ c_col, int i, int key,
+                                        int *flags)
+{
+    if constexpr (kMap) return __ldg(pmap + base + t);
+    return c_position(c_rpt, c_col, i, key, flags);
+}
+
+constexpr int kGradBatch = 8;      // chain steps whose operands are loaded together
+constexpr int kGradShortMax = 64;  // dA chains longer than this are folded by a warp
+
+// dA, chains of at most kGradShortMax terms: one thread per A entry p = (i, j), folding
+// B row j in order, kGradBatch terms' operands loaded ahead of their FMAs.  Longer chains
+// are listed for k_grad_a_long.
 template <typename T, bool kMap>
-__global__ void __launch_bounds__(256) k_grad_a(const int *__restrict__ arpt, const int *__restrict__ acol, int M,
-                                                 const int *__restrict__ brpt, const int *__restrict__ bcol,
-                                                 const T *__restrict__ bval, const int *__restrict__ c_rpt,
-                                                 const int *__restrict__ c_col, const T *__restrict__ dc,
-                                                 const long long *__restrict__ pos_base, const int *__restrict__ pmap,
-                                                 T *__restrict__ da, int *flags)
+__global__ void __launch_bounds__(256) k_grad_a_short(const int *__restrict__ acol, long long nnz_a,
+                                                       const int *__restrict__ arow, const int *__restrict__ brpt,
+                                                       const int *__restrict__ bcol, const T *__restrict__ bval,
+                                                       const int *__restrict__ c_rpt, const int *__restrict__ c_col,
+                                                       const T *__restrict__ dc, const long long *__restrict__ pos_base,
+                                                       const int *__restrict__ pmap, T *__restrict__ da,
+                                                       int *__restrict__ long_list, int *long_count, int *flags)
 {
     using AccT = Acc<T>;
-    const long long w0 = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
-    const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
-    for (long long i = w0; i < M; i += nw) {
-        const int a0 = __ldg(arpt + i), a1 = __ldg(arpt + i + 1);
-        for (int p = a0 + lane_id(); p < a1; p += 32) {
-            const int j = __ldg(acol + p);
-            const int b0 = __ldg(brpt + j), b1 = __ldg(brpt + j + 1);
-            typename AccT::S s = AccT::zero();
-            const long long base = kMap ? __ldg(pos_base + p) : 0;
-            for (int q = b0; q < b1; ++q) {
-                int pos;
-                if (kMap) pos = __ldg(pmap + base + (q - b0));
-                else pos = c_position(c_rpt, c_col, (int)i, __ldg(bcol + q), flags);
-                const T d = pos >= 0 ? __ldg(dc + pos) : T(0);
-                s = AccT::step(s, __ldg(bval + q), d);
-            }
-            da[p] = AccT::fin(s);
+    for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < nnz_a;
+         p += (long long)gridDim.x * blockDim.x) {
+        const int j = __ldg(acol + p);
+        const int b0 = __ldg(brpt + j), b1 = __ldg(brpt + j + 1);
+        if (b1 - b0 > kGradShortMax) {
+            long_list[atomicAdd(long_count, 1)] = (int)p;
+            continue;
         }
+        const long long base = kMap ? __ldg(pos_base + p) : 0;
+        const int i = kMap ? 0 : __ldg(arow + p);
+        typename AccT::S s = AccT::zero();
+        for (int q0 = b0; q0 < b1; q0 += kGradBatch) {
+            int pos[kGradBatch];
+            T bv[kGradBatch], d[kGradBatch];
+#pragma unroll
+            for (int u = 0; u < kGradBatch; ++u)
+                pos[u] = q0 + u < b1 ? prod_pos<kMap>(pmap, base, q0 + u - b0, c_rpt, c_col, i,
+                                                      kMap ? 0 : __ldg(bcol + q0 + u), flags)
+                                     : -1;
+#pragma unroll
+            for (int u = 0; u < kGradBatch; ++u) {
+                bv[u] = q0 + u < b1 ? __ldg(bval + q0 + u) : T(0);
+                d[u] = pos[u] >= 0 ? __ldg(dc + pos[u]) : T(0);
+            }
+#pragma unroll
+            for (int u = 0; u < kGradBatch; ++u)
+                if (q0 + u < b1) s = AccT::step(s, bv[u], d[u]);
+        }
+        da[p] = AccT::fin(s);
     }
 }
 
-// dB: one warp per row j of B, lanes over the row's entries, each folding the A entries
-// of column j in ascending row order.
+// dA, long chains: one warp per listed A entry.  The lanes load the operands of the next
+// two batches of 32 terms (positions and B values coalesced, dC gathered in parallel)
+// while lane 0 folds the current 32 from shared memory, in order.
+template <typename T, bool kMap>
+__global__ void __launch_bounds__(256) k_grad_a_long(const int *__restrict__ acol, const int *__restrict__ arow,
+                                                      const int *__restrict__ brpt, const int *__restrict__ bcol,
+                                                      const T *__restrict__ bval, const int *__restrict__ c_rpt,
+                                                      const int *__restrict__ c_col, const T *__restrict__ dc,
+                                                      const long long *__restrict__ pos_base,
+                                                      const int *__restrict__ pmap, T *__restrict__ da,
+                                                      const int *__restrict__ long_list, const int *long_count,
+                                                      int *flags)
+{
+    using AccT = Acc<T>;
+    __shared__ T s_b[256 / 32][2][32];
+    __shared__ T s_d[256 / 32][2][32];
+    const int lane = lane_id();
+    const int warp = threadIdx.x >> 5;
+    const int count = *long_count;
+    const long long w0 = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+    const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
+    for (long long it = w0; it < count; it += nw) {
+        const int p = __ldg(long_list + it);
+        const int j = __ldg(acol + p);
+        const int b0 = __ldg(brpt + j), b1 = __ldg(brpt + j + 1);
+        const long long base = kMap ? __ldg(pos_base + p) : 0;
+        const int i = kMap ? 0 : __ldg(arow + p);
+        auto gather = [&](int q, T &bv, T &d) {
+            bv = T(0);
+            d = T(0);
+            if (q < b1) {
+                const int pos = prod_pos<kMap>(pmap, base, q - b0, c_rpt, c_col, i, kMap ? 0 : __ldg(bcol + q), flags);
+                bv = __ldg(bval + q);
+                d = pos >= 0 ? __ldg(dc + pos) : T(0);
+            }
+        };
+        T nb, nd, nb2, nd2;
+        gather(b0 + lane, nb, nd);
+        gather(b0 + 32 + lane, nb2, nd2);
+        typename AccT::S s = AccT::zero();
+        int buf = 0;
+        for (int q = b0; q < b1; q += 32) {
+            s_b[warp][buf][lane] = nb;
+            s_d[warp][buf][lane] = nd;
+            __syncwarp();
+            nb = nb2;
+            nd = nd2;
+            gather(q + 64 + lane, nb2, nd2);
+            if (lane == 0) {
+                const int m = min(32, b1 - q);
+                for (int u = 0; u < m; ++u) s = AccT::step(s, s_b[warp][buf][u], s_d[warp][buf][u]);
+            }
+            buf ^= 1;
+        }
+        if (lane == 0) da[p] = AccT::fin(s);
+        __syncwarp();
+    }
+}
+
+// dB: one warp per row j of B, lanes over the row's entries q, each folding the A entries
+// of column j in ascending row order.  All lanes walk the same column entries, so the
+// warp loads 32 of them at once (one per lane) and shares them by shuffle; each lane then
+// loads kGradBatch terms' positions and dC values ahead of its FMAs.
 template <typename T, bool kMap>
 __global__ void __launch_bounds__(256) k_grad_b(int K, const int *__restrict__ brpt, const int *__restrict__ bcol,
                                                  const T *__restrict__ aval, const int *__restrict__ at_ptr,
@@ -159,23 +248,49 @@ __global__ void __launch_bounds__(256) k_grad_b(int K, const int *__restrict__ b
                                                  const int *__restrict__ pmap, T *__restrict__ db, int *flags)
 {
     using AccT = Acc<T>;
+    const int lane = lane_id();
     const long long w0 = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
     const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
     for (long long j = w0; j < K; j += nw) {
         const int b0 = __ldg(brpt + j), b1 = __ldg(brpt + j + 1);
         const int e0 = __ldg(at_ptr + j), e1 = __ldg(at_ptr + j + 1);
-        for (int q = b0 + lane_id(); q < b1; q += 32) {
-            const int key = kMap ? 0 : __ldg(bcol + q);
+        for (int qb = b0; qb < b1; qb += 32) {
+            const int q = qb + lane;
+            const bool qv = q < b1;
+            const int key = (!kMap && qv) ? __ldg(bcol + q) : 0;
             typename AccT::S s = AccT::zero();
-            for (int e = e0; e < e1; ++e) {
-                const int p = __ldg(at_ent + e);
-                int pos;
-                if (kMap) pos = __ldg(pmap + __ldg(pos_base + p) + (q - b0));
-                else pos = c_position(c_rpt, c_col, __ldg(arow + p), key, flags);
-                const T d = pos >= 0 ? __ldg(dc + pos) : T(0);
-                s = AccT::step(s, __ldg(aval + p), d);
+            for (int eb = e0; eb < e1; eb += 32) {
+                // one column entry per lane: its A entry, row, value and product base
+                int pe = 0, re = 0;
+                long long be = 0;
+                T ae = T(0);
+                if (eb + lane < e1) {
+                    pe = __ldg(at_ent + eb + lane);
+                    ae = __ldg(aval + pe);
+                    if (kMap) be = __ldg(pos_base + pe);
+                    else re = __ldg(arow + pe);
+                }
+                const int m = min(32, e1 - eb);
+                for (int t0 = 0; t0 < m; t0 += kGradBatch) {
+                    int pos[kGradBatch];
+                    T a[kGradBatch], d[kGradBatch];
+#pragma unroll
+                    for (int u = 0; u < kGradBatch; ++u) {
+                        const int src = min(t0 + u, 31);
+                        const long long bu = kMap ? __shfl_sync(kFull, be, src) : 0;
+                        const int ru = kMap ? 0 : __shfl_sync(kFull, re, src);
+                        a[u] = shfl(ae, src);
+                        pos[u] = (qv && t0 + u < m) ? prod_pos<kMap>(pmap, bu, q - b0, c_rpt, c_col, ru, key, flags)
+                                                    : -1;
+                    }
+#pragma unroll
+                    for (int u = 0; u < kGradBatch; ++u) d[u] = pos[u] >= 0 ? __ldg(dc + pos[u]) : T(0);
+#pragma unroll
+                    for (int u = 0; u < kGradBatch; ++u)
+                        if (t0 + u < m) s = AccT::step(s, a[u], d[u]);
+                }
             }
-            db[q] = AccT::fin(s);
+            if (qv) db[q] = AccT::fin(s);
         }
     }
 }
@@ -303,14 +418,29 @@ int run_backward(ops_handle_s *h, int M, int K, const int *a_rpt, const int *a_c
     const BackwardPlan &pl = h->bwd;
     const int sms = h->num_sms;
     int *flags = &h->info->flags;
-    if (da && M > 0) {
-        if (pl.with_map)
-            k_grad_a<T, true><<<grid_of(M, 8, sms * 8), 256, 0, st>>>(a_rpt, a_col, M, b_rpt, b_col, b_val, c_rpt, c_col,
-                                                                      dc, pl.pos_base, pl.pmap, da, flags);
-        else
-            k_grad_a<T, false><<<grid_of(M, 8, sms * 8), 256, 0, st>>>(a_rpt, a_col, M, b_rpt, b_col, b_val, c_rpt,
-                                                                       c_col, dc, pl.pos_base, pl.pmap, da, flags);
+    if (da && pl.nnz_a > 0) {
+        // thread per A entry for short chains; the long ones are listed and get a warp each
+        int *long_list = nullptr;
+        OPS_CUDA(h, cudaMallocFromPoolAsync(reinterpret_cast<void **>(&long_list), sizeof(int) * pl.nnz_a, h->pool,
+                                            st));
+        OPS_CUDA(h, cudaMemsetAsync(&h->info->d_cursor, 0, sizeof(int), st));
+        const int g1 = grid_of(pl.nnz_a, 256, sms * 16);
+        if (pl.with_map) {
+            k_grad_a_short<T, true><<<g1, 256, 0, st>>>(a_col, pl.nnz_a, pl.arow, b_rpt, b_col, b_val, c_rpt, c_col, dc,
+                                                        pl.pos_base, pl.pmap, da, long_list, &h->info->d_cursor, flags);
+            k_grad_a_long<T, true><<<sms * 8, 256, 0, st>>>(a_col, pl.arow, b_rpt, b_col, b_val, c_rpt, c_col, dc,
+                                                            pl.pos_base, pl.pmap, da, long_list, &h->info->d_cursor,
+                                                            flags);
+        } else {
+            k_grad_a_short<T, false><<<g1, 256, 0, st>>>(a_col, pl.nnz_a, pl.arow, b_rpt, b_col, b_val, c_rpt, c_col,
+                                                         dc, pl.pos_base, pl.pmap, da, long_list, &h->info->d_cursor,
+                                                         flags);
+            k_grad_a_long<T, false><<<sms * 8, 256, 0, st>>>(a_col, pl.arow, b_rpt, b_col, b_val, c_rpt, c_col, dc,
+                                                             pl.pos_base, pl.pmap, da, long_list, &h->info->d_cursor,
+                                                             flags);
+        }
         OPS_CUDA(h, cudaGetLastError());
+        OPS_CUDA(h, cudaFreeAsync(long_list, st));
     }
     if (db && K > 0) {
         if (pl.with_map)
