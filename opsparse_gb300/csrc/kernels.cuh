@@ -446,18 +446,18 @@ __global__ void __launch_bounds__(256) k_reg_rows(SpgemmArgs<T> g, const int *__
 // ==================================================================================
 // Writes the n compacted (column, value) entries of a warp-hash row to C in column order:
 // keys (column << 8 | slot) are sorted in registers by the warp bitonic network.
-template <int PER, typename T>
+template <int PER, typename T, typename KT>
 __device__ __forceinline__ void warp_table_sort_write(const SpgemmArgs<T> &g, const int *keys,
                                                       const typename Acc<T>::S *vals, int n, int off)
 {
     const int lane = lane_id();
-    unsigned long long x[PER];
+    KT x[PER];
 #pragma unroll
     for (int i = 0; i < PER; ++i) {
         const int e = i * 32 + lane;  // any arrangement will do: the network sorts it
-        x[i] = e < n ? (((unsigned long long)(unsigned)keys[e] << 8) | (unsigned)e) : ~0ull;
+        x[i] = e < n ? (((KT)(unsigned)keys[e] << 8) | (KT)(unsigned)e) : ~KT(0);
     }
-    warp_bitonic_blocked<PER, unsigned long long>(x);
+    warp_bitonic_blocked<PER, KT>(x);
 #pragma unroll
     for (int i = 0; i < PER; ++i) {
         const int e = lane * PER + i;
@@ -505,15 +505,18 @@ __global__ void __launch_bounds__(kWarpRowsThreads) k_warp_rows(SpgemmArgs<T> g,
         } else {
             n_expect = __ldg(g.row_flop + r);
         }
-        const int log_ts = max(5, ceil_log2(2 * max(n_expect, 1)));
-        const int ts = 1 << log_ts;
-        for (int i = lane; i < ts; i += 32) {
+        // numeric knows the row's output count: 4 slots per output where the table has
+        // room (fewer probe collisions), at least 2
+        const int log_ts = kNum ? min(ceil_log2_c(TMAX), max(5, ceil_log2(4 * max(n_expect, 1))))
+                                : max(5, ceil_log2(2 * max(n_expect, 1)));
+        const int row_products = kNum ? __ldg(g.row_flop + r) : n_expect;
+        const bool rowwise = row_products >= 16 * (a1 - a0);
+        for (int i = lane; i < (1 << log_ts); i += 32) {
             keys[i] = kEmpty;
             if constexpr (kNum) vals[i] = AccT::zero();
         }
         __syncwarp();
         int cnt = 0;
-        const int row_products = kNum ? __ldg(g.row_flop + r) : n_expect;
         if constexpr (!kNum) {
             // counting is order-free: kUnroll chunks of 32 products have their column
             // loads in flight together before the claims
@@ -557,7 +560,7 @@ __global__ void __launch_bounds__(kWarpRowsThreads) k_warp_rows(SpgemmArgs<T> g,
                     }
                 }
             }
-        } else if (row_products >= 16 * (a1 - a0)) {
+        } else if (rowwise) {
             // long B rows: one B row per step, every lane owns a distinct key; four
             // B rows' operands are loaded ahead of their steps
             warp_rowwise_products_pf<4, kNum, T>(a0, a1, g.acol, g.aval, g.brpt, g.bcol, g.bval,
@@ -601,7 +604,7 @@ __global__ void __launch_bounds__(kWarpRowsThreads) k_warp_rows(SpgemmArgs<T> g,
         } else {
             // In-place compaction: block b of 32 slots writes to positions < 32*(b+1).
             int n = 0;
-            for (int base = 0; base < ts; base += 32) {
+            for (int base = 0; base < (1 << log_ts); base += 32) {
                 const int kk = keys[base + lane];
                 const S vv = vals[base + lane];
                 const bool occ = kk != kEmpty;
@@ -625,10 +628,15 @@ __global__ void __launch_bounds__(kWarpRowsThreads) k_warp_rows(SpgemmArgs<T> g,
                     g.c_col[off + rank] = ke;
                     g.c_val[off + rank] = AccT::fin(vals[e]);
                 }
+            } else if (g.N <= (1 << 24)) {  // (column << 8 | slot) fits 32 bits
+                if (nw <= 128)
+                    warp_table_sort_write<4, T, unsigned>(g, keys, vals, nw, off);
+                else if (nw <= 256)
+                    warp_table_sort_write<8, T, unsigned>(g, keys, vals, nw, off);
             } else if (nw <= 128) {
-                warp_table_sort_write<4, T>(g, keys, vals, nw, off);
+                warp_table_sort_write<4, T, unsigned long long>(g, keys, vals, nw, off);
             } else if (nw <= 256) {
-                warp_table_sort_write<8, T>(g, keys, vals, nw, off);
+                warp_table_sort_write<8, T, unsigned long long>(g, keys, vals, nw, off);
             } else {  // not reached: numeric rows here have at most TMAX/2 outputs
                 if (lane == 0) atomicOr(&g.info->flags, kErrCountMismatch);
             }
