@@ -369,7 +369,7 @@ def run_ours(args, desc, dt, data, n, rank, world, local_rank):
         "gpu_launches": launches,
         "clocks": clk.summary(),
     }
-    if dt == "f64" and world == 1:
+    if dt == "f64" and world == 1 and args.reference_gpu:
         line["reference_gpu"] = reference_gpu(A, B, n, P, nnz_c, t_ms, flush)
     if args.cpu_baseline and world == 1:
         t_cpu, cores = cpu_baseline(data, n)
@@ -391,6 +391,8 @@ def main():
                              "backward_f32"])
     ap.add_argument("--batch", type=int, default=4096, help="problems in the batched workload")
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
+    ap.add_argument("--no-reference-gpu", dest="reference_gpu", action="store_false",
+                    help="skip timing OpSparse's own kernels on the GPU (for profiling runs)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
