@@ -51,7 +51,7 @@ struct BescShape {
 };
 
 using BescE1 = BescShape<128, 8, 1024, 4>;    // E1 rows of more than kSplitNnz outputs
-using BescMid = BescShape<256, 16, 1280, 3>;  // E2 rows of at most 4,096 products
+using BescMid = BescShape<256, 16, 1280, 4>;  // E2 rows of at most 4,096 products
 
 __device__ __forceinline__ int bpad(int e) { return e + (e >> 5); }
 

@@ -40,14 +40,16 @@ struct EscShape {
     static constexpr int kDigits = 256;
     // numeric: keys x2 (u32), ids x2 (u16), owner per product (u16), per-warp digit
     // counters, A-entry scan + B row starts
-    static constexpr size_t kNumericSmem = (size_t)PCAP * (4 + 4 + 2 + 2 + 2) + (size_t)kWarps * kDigits * 4 +
+    // radix histograms: 16-bit counters (a warp's slice and every offset are < 2^16)
+    static constexpr size_t kNumericSmem = (size_t)PCAP * (4 + 4 + 2 + 2 + 2) + (size_t)kWarps * kDigits * 2 +
                                            (size_t)ACAP * 8 + 32 * 4 + 64;
+    static_assert(PCAP < 65536, "16-bit radix offsets");
     static constexpr size_t kSymbolicSmem = (size_t)kTable * 4 + (size_t)ACAP * 8 + 32 * 4 + 64;
 };
 
 using EscSmall = EscShape<128, 1024, 1024>;
 using EscMid = EscShape<256, 4096, 1280>;     // 75,968 B numeric: three CTAs per SM
-using EscLarge = EscShape<512, 13312, 2560>;  // 223,424 B numeric: one CTA per SM
+using EscLarge = EscShape<1024, 13312, 2560>;  // 223,424 B numeric: one 1024-thread CTA per SM
 
 constexpr int kUnroll = 4;  // chunks (expansion) or products (fold) with loads in flight together
 
@@ -159,14 +161,15 @@ __global__ void __launch_bounds__(Shape::kThreads) k_esc_rows(SpgemmArgs<T> g, c
     unsigned char *p = smem_raw;
     unsigned *key0 = nullptr, *key1 = nullptr;
     unsigned short *id0 = nullptr, *id1 = nullptr, *own = nullptr;
-    int *hist = nullptr, *table = nullptr;
+    unsigned short *hist = nullptr;
+    int *table = nullptr;
     if constexpr (kNum) {
         key0 = reinterpret_cast<unsigned *>(p);
         p += sizeof(unsigned) * PCAP;
         key1 = reinterpret_cast<unsigned *>(p);
         p += sizeof(unsigned) * PCAP;
-        hist = reinterpret_cast<int *>(p);
-        p += sizeof(int) * NW * Shape::kDigits;
+        hist = reinterpret_cast<unsigned short *>(p);
+        p += sizeof(unsigned short) * NW * Shape::kDigits;
     } else {
         table = reinterpret_cast<int *>(p);
         p += sizeof(int) * Shape::kTable;
@@ -277,7 +280,7 @@ __global__ void __launch_bounds__(Shape::kThreads) k_esc_rows(SpgemmArgs<T> g, c
             const int per = (n + NW - 1) / NW;
             const int rb = min(n, warp * per);
             const int re = min(n, rb + per);
-            int *wh = hist + warp * Shape::kDigits;
+            unsigned short *wh = hist + warp * Shape::kDigits;
             for (int pass = 0; pass < passes; ++pass) {
                 const int shift = 8 * pass;
                 for (int d = lane; d < Shape::kDigits; d += 32) wh[d] = 0;
@@ -308,7 +311,7 @@ __global__ void __launch_bounds__(Shape::kThreads) k_esc_rows(SpgemmArgs<T> g, c
 #pragma unroll
                 for (int e = 0; e < kPer; ++e) {
                     const int i = tid * kPer + e;
-                    hist[(i % NW) * Shape::kDigits + i / NW] = run;
+                    hist[(i % NW) * Shape::kDigits + i / NW] = (unsigned short)run;
                     run += v[e];
                 }
                 __syncthreads();
@@ -326,7 +329,7 @@ __global__ void __launch_bounds__(Shape::kThreads) k_esc_rows(SpgemmArgs<T> g, c
                     base = __shfl_sync(kFull, base, leader);
                     const int pos = base + __popc(peers & lanemask_lt());
                     __syncwarp();
-                    if (lane == leader && valid) wh[d] = base + __popc(peers);
+                    if (lane == leader && valid) wh[d] = (unsigned short)(base + __popc(peers));
                     if (valid) {
                         kout[pos] = key;
                         iout[pos] = id;

@@ -265,7 +265,7 @@ __device__ __forceinline__ void cmp_swap3(K &ka, T &aa, T &ba, K &kb, T &ab, T &
 }
 
 template <typename T>
-__global__ void __launch_bounds__(kSmallThreads) k_small_rows(SpgemmArgs<T> g, int r8)
+__global__ void __launch_bounds__(kSmallThreads, 4) k_small_rows(SpgemmArgs<T> g, int r8)
 {
     using AccT = Acc<T>;
     constexpr int U = kSmallFlopMax;
