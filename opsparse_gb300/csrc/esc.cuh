@@ -464,41 +464,45 @@ struct PickE2 {
 };
 
 // Orders a class list by product count, largest first, so that with dynamic row
-// scheduling the longest rows start first (longest-processing-time order).  One CTA,
-// bitonic sort of (row_flop, row) in shared memory; lists longer than kLptMax stay as
-// they are.
+// scheduling the longest rows start first (longest-processing-time order).  One CTA;
+// lists longer than kLptMax stay as they are.
 constexpr int kLptMax = 4096;
 
 static __global__ void __launch_bounds__(1024) k_sort_heavy_first(int *list, const int *count_ptr,
                                                            const int *__restrict__ row_flop)
 {
-    __shared__ unsigned long long s_e[kLptMax];
+    // Rows are grouped by product count in quarter-octave buckets, largest first: one
+    // histogram, one scan, one scatter.  Scheduling only needs the heavy rows early; the
+    // order inside a bucket is free (every row's result is independent of it).
+    constexpr int kBuckets = 128;
+    __shared__ int s_rows[kLptMax];
+    __shared__ unsigned char s_bucket[kLptMax];
+    __shared__ int s_next[kBuckets];
     const int n = *count_ptr;
     if (n <= 1 || n > kLptMax) return;
-    int m = 1;
-    while (m < n) m <<= 1;
-    for (int i = threadIdx.x; i < m; i += blockDim.x) {
-        // descending flop == ascending (~flop); ties by row id for determinism
-        s_e[i] = i < n ? ((unsigned long long)(0xffffffffu - (unsigned)row_flop[list[i]]) << 32) | (unsigned)list[i]
-                       : ~0ull;
+    for (int i = threadIdx.x; i < kBuckets; i += blockDim.x) s_next[i] = 0;
+    __syncthreads();
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const int r = list[i];
+        const unsigned f = (unsigned)max(row_flop[r], 1);
+        const int lz = 31 - __clz(f);  // floor(log2 f)
+        const int frac = lz >= 2 ? (int)((f >> (lz - 2)) & 3u) : 0;
+        const int b = kBuckets - 1 - min(kBuckets - 1, 4 * lz + frac);
+        s_rows[i] = r;
+        s_bucket[i] = (unsigned char)b;
+        atomicAdd(&s_next[b], 1);
     }
     __syncthreads();
-    for (int k = 2; k <= m; k <<= 1) {
-        for (int j = k >> 1; j > 0; j >>= 1) {
-            for (int i = threadIdx.x; i < m; i += blockDim.x) {
-                const int ixj = i ^ j;
-                if (ixj > i) {
-                    const unsigned long long a = s_e[i], b = s_e[ixj];
-                    if ((a > b) == ((i & k) == 0)) {
-                        s_e[i] = b;
-                        s_e[ixj] = a;
-                    }
-                }
-            }
-            __syncthreads();
+    if (threadIdx.x == 0) {
+        int run = 0;
+        for (int b = 0; b < kBuckets; ++b) {
+            const int c = s_next[b];
+            s_next[b] = run;
+            run += c;
         }
     }
-    for (int i = threadIdx.x; i < n; i += blockDim.x) list[i] = (int)(s_e[i] & 0xffffffffu);
+    __syncthreads();
+    for (int i = threadIdx.x; i < n; i += blockDim.x) list[atomicAdd(&s_next[s_bucket[i]], 1)] = s_rows[i];
 }
 
 }  // namespace opsg

@@ -29,7 +29,9 @@ struct WsortShape {
     static constexpr int kMax = 32 * PMAX;                     // products per row, at most
     static constexpr int kWarps = PMAX <= 4 ? 8 : 4;           // warps per CTA
     static constexpr int kThreads = 32 * kWarps;
-    static constexpr int kMinBlocks = PMAX >= 32 ? 4 : 1;      // caps the 32-key variant at 128 registers
+    // CTAs per SM the registers must allow: 4 for both the 128-key variant (8 warps per
+    // CTA, 64 registers) and the 32-key symbolic variant (128 registers)
+    static constexpr int kMinBlocks = PMAX >= 32 ? 4 : (PMAX <= 4 ? 4 : 1);
     static constexpr int kIdBits = PMAX <= 4 ? 7 : (PMAX <= 8 ? 8 : (PMAX <= 16 ? 9 : 10));
     static constexpr int kKeySlots = kMax + kMax / 32;         // padded key array
     static constexpr int kHeadSlots = kMax + 32;               // run heads + end marker
@@ -110,8 +112,8 @@ __device__ __forceinline__ int wsort_row(const SpgemmArgs<T> &g, int flop, KT *s
     return total;
 }
 
-// One warp per listed row (flop <= 32*PMAX).  Rows of at most 128 products sort 128 keys,
-// at most 256 sort 256, and so on up to 32*PMAX (PMAX = 32 is used for the symbolic
+// One warp per listed row (flop <= 32*PMAX).  Rows of at most 64 products sort 64 keys,
+// at most 128 sort 128, and so on up to 32*PMAX (PMAX = 32 is used for the symbolic
 // count of rows of up to 1024 products).  The row count is read from
 // device memory, so lists split on the device need no host round trip.
 template <int PMAX, bool kNum, typename T, typename KT>
@@ -214,7 +216,9 @@ __global__ void __launch_bounds__(WsortShape<PMAX>::kThreads, WsortShape<PMAX>::
         // the smallest power-of-two network that holds the row (rows are listed here
         // only if flop <= 32*PMAX)
         int total = 0;
-        if (flop <= 128) {
+        if (flop <= 64) {
+            total = wsort_row<2, kIdBits, kNum, T, KT>(g, flop, skey, heads, sa, sb, off, n_expect);
+        } else if (flop <= 128) {
             total = wsort_row<4, kIdBits, kNum, T, KT>(g, flop, skey, heads, sa, sb, off, n_expect);
         } else if constexpr (PMAX >= 8) {
             if (flop <= 256) {
