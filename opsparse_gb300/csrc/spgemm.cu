@@ -188,7 +188,11 @@ int launch_classes(ops_handle_s *h, const SpgemmArgs<T> &g, cudaStream_t st)
         return cudaEventRecord(h->ev_x_join[x], h->side_x[x]) == cudaSuccess &&
                cudaStreamWaitEvent(into, h->ev_x_join[x], 0) == cudaSuccess;
     };
-    for (int c = 0; c < kNumClasses; ++c) {
+    // heaviest classes first: their long kernels then overlap the light classes instead
+    // of forming the tail of the phase
+    constexpr int kOrder[kNumClasses] = {kClsE2, kClsD, kClsE1, kClsW, kClsR32, kClsR16, kClsR8};
+    for (int oi = 0; oi < kNumClasses; ++oi) {
+        const int c = kOrder[oi];
         const int n = h->counts[c];
         if (n <= 0) continue;
         if (!kNum && c == kClsR8) continue;  // R8 rows are counted inside k_setup
