@@ -56,56 +56,118 @@ struct Segment {
     ops_handle_s *h = nullptr;  // per-segment plan (classes, workspace)
 };
 
-// per-problem intermediate products: one CTA per problem
-__global__ void k_batch_flop(const Item *__restrict__ items, int n, unsigned long long *__restrict__ flop)
+// The batch helpers walk flattened element spaces: a segment's A entries (or rows, or
+// B entries, or B rows) are the concatenation of its problems', and each problem's share
+// starts at its base offset.  A CTA takes a fixed chunk of the space, finds the problem
+// holding the chunk's first element by binary search over the bases, and walks forward,
+// so a 65,536-row problem is spread over many CTAs instead of one.
+enum Field : int { kFARpt, kFACol, kFBRpt, kFBCol };
+constexpr int kFlatChunk = 4096;
+
+template <int F>
+__device__ __forceinline__ long long field_base(const Item &it)
 {
-    for (int b = blockIdx.x; b < n; b += gridDim.x) {
-        const Item it = items[b];
-        unsigned long long s = 0;
-        for (int r = threadIdx.x; r < it.rows; r += blockDim.x) {
-            for (int p = it.a_rpt[r]; p < it.a_rpt[r + 1]; ++p) {
-                const int j = it.a_col[p];
-                if ((unsigned)j < (unsigned)it.cols_a) s += (unsigned long long)(it.b_rpt[j + 1] - it.b_rpt[j]);
+    if constexpr (F == kFARpt) return it.row_base;
+    if constexpr (F == kFACol) return it.a_base;
+    if constexpr (F == kFBRpt) return it.k_base;
+    return it.b_base;
+}
+
+// Last problem in [0, count) whose base is <= e (bases non-decreasing, base(0) == 0).
+template <int F>
+__device__ __forceinline__ int flat_problem(const Item *__restrict__ items, int count, long long e)
+{
+    int lo = 0, hi = count;
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (field_base<F>(items[mid]) <= e) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
+// per-problem intermediate products, over all A entries of all problems (a_base holds the
+// problems' offsets in that concatenation while this runs); flop[] must start at zero
+__global__ void k_batch_flop(const Item *__restrict__ items, int n, long long total, unsigned long long *flop)
+{
+    __shared__ int s_b;
+    const int lane = lane_id();
+    for (long long c0 = (long long)blockIdx.x * kFlatChunk; c0 < total; c0 += (long long)gridDim.x * kFlatChunk) {
+        if (threadIdx.x == 0) s_b = flat_problem<kFACol>(items, n, c0);
+        __syncthreads();
+        int b = s_b;
+        const long long c1 = min(total, c0 + kFlatChunk);
+        for (long long e0 = c0; e0 < c1; e0 += blockDim.x) {
+            const long long e = e0 + threadIdx.x;
+            unsigned long long f = 0;
+            if (e < c1) {
+                while (b + 1 < n && items[b + 1].a_base <= e) ++b;
+                const Item &it = items[b];
+                const int j = it.a_col[e - it.a_base];
+                if ((unsigned)j < (unsigned)it.cols_a) f = (unsigned long long)(it.b_rpt[j + 1] - it.b_rpt[j]);
+            }
+            // a warp's entries almost always belong to one problem: one atomic then
+            const int bb = e < c1 ? b : -1;
+            const int b0 = __shfl_sync(kFull, bb, 0);
+            if (__all_sync(kFull, bb == b0)) {
+                unsigned long long sum = f;
+#pragma unroll
+                for (int d = 16; d >= 1; d >>= 1) sum += __shfl_xor_sync(kFull, sum, d);
+                if (lane == 0 && b0 >= 0 && sum) atomicAdd(&flop[b0], sum);
+            } else if (bb >= 0 && f) {
+                atomicAdd(&flop[bb], f);
             }
         }
-#pragma unroll
-        for (int d = 16; d >= 1; d >>= 1) s += __shfl_xor_sync(kFull, s, d);
-        __shared__ unsigned long long part[32];
-        if (lane_id() == 0) part[threadIdx.x >> 5] = s;
         __syncthreads();
-        if (threadIdx.x == 0) {
-            unsigned long long t = 0;
-            for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += part[w];
-            flop[b] = t;
+    }
+}
+
+// Builds one segment's block-diagonal structure field F: A's row pointers (shifted to the
+// problem's first A entry), A's columns (shifted to the problem's first B row), B's row
+// pointers (shifted to its first B entry), or B's columns (local).
+template <int F>
+__global__ void k_batch_gather_field(const Item *__restrict__ items, int count, long long total, int *__restrict__ dst)
+{
+    __shared__ int s_b;
+    for (long long c0 = (long long)blockIdx.x * kFlatChunk; c0 < total; c0 += (long long)gridDim.x * kFlatChunk) {
+        if (threadIdx.x == 0) s_b = flat_problem<F>(items, count, c0);
+        __syncthreads();
+        int b = s_b;
+        const long long c1 = min(total, c0 + kFlatChunk);
+        for (long long e = c0 + threadIdx.x; e < c1; e += blockDim.x) {
+            while (b + 1 < count && field_base<F>(items[b + 1]) <= e) ++b;
+            const Item &it = items[b];
+            const long long i = e - field_base<F>(it);
+            if constexpr (F == kFARpt) dst[e] = (int)(it.a_base + it.a_rpt[i]);
+            if constexpr (F == kFACol) dst[e] = it.a_col[i] + it.k_base;
+            if constexpr (F == kFBRpt) dst[e] = (int)(it.b_base + it.b_rpt[i]);
+            if constexpr (F == kFBCol) dst[e] = it.b_col[i];
         }
         __syncthreads();
     }
 }
 
-// Builds one segment's block-diagonal structure (rpt, col); one CTA per problem.
-__global__ void k_batch_gather_structure(const Item *__restrict__ items, int first, int count, int *a_rpt, int *a_col,
-                                         int *b_rpt, int *b_col)
+// Values of one segment's A (F = kFACol) or B (F = kFBCol) entries.
+template <int F, typename T>
+__global__ void k_batch_gather_vals(const Item *__restrict__ items, int count, long long total, T *__restrict__ dst)
 {
-    for (int b = blockIdx.x; b < count; b += gridDim.x) {
-        const Item it = items[first + b];
-        for (int r = threadIdx.x; r < it.rows; r += blockDim.x) a_rpt[it.row_base + r] = (int)(it.a_base + it.a_rpt[r]);
-        for (long long p = threadIdx.x; p < it.a_nnz; p += blockDim.x) a_col[it.a_base + p] = it.a_col[p] + it.k_base;
-        for (int r = threadIdx.x; r < it.cols_a; r += blockDim.x) b_rpt[it.k_base + r] = (int)(it.b_base + it.b_rpt[r]);
-        for (long long p = threadIdx.x; p < it.b_nnz; p += blockDim.x) b_col[it.b_base + p] = it.b_col[p];
+    __shared__ int s_b;
+    for (long long c0 = (long long)blockIdx.x * kFlatChunk; c0 < total; c0 += (long long)gridDim.x * kFlatChunk) {
+        if (threadIdx.x == 0) s_b = flat_problem<F>(items, count, c0);
+        __syncthreads();
+        int b = s_b;
+        const long long c1 = min(total, c0 + kFlatChunk);
+        for (long long e = c0 + threadIdx.x; e < c1; e += blockDim.x) {
+            while (b + 1 < count && field_base<F>(items[b + 1]) <= e) ++b;
+            const Item &it = items[b];
+            const T *src = static_cast<const T *>(F == kFACol ? it.a_val : it.b_val);
+            dst[e] = src[e - field_base<F>(it)];
+        }
+        __syncthreads();
     }
 }
 
-template <typename T>
-__global__ void k_batch_gather_values(const Item *__restrict__ items, int first, int count, T *a_val, T *b_val)
-{
-    for (int b = blockIdx.x; b < count; b += gridDim.x) {
-        const Item it = items[first + b];
-        const T *av = static_cast<const T *>(it.a_val);
-        const T *bv = static_cast<const T *>(it.b_val);
-        for (long long p = threadIdx.x; p < it.a_nnz; p += blockDim.x) a_val[it.a_base + p] = av[p];
-        for (long long p = threadIdx.x; p < it.b_nnz; p += blockDim.x) b_val[it.b_base + p] = bv[p];
-    }
-}
+int flat_grid(long long total, int sms) { return (int)std::max<long long>(1, std::min<long long>((total + kFlatChunk - 1) / kFlatChunk, (long long)sms * 16)); }
 
 // Per-problem row_ptr rebased to start at 0, written to the result arena.
 __global__ void k_batch_rebase(const Item *__restrict__ items, int first, int count, const int *__restrict__ c_rpt,
@@ -211,6 +273,11 @@ extern "C" int ops_batch_create(ops_handle_t h, int dtype, int32_t count, const 
     };
     // 1. per-problem products (device), then segmentation on the host
     std::vector<unsigned long long> flop(std::max(count, 1), 0ull);
+    long long total_a = 0;
+    for (Item &it : b->items) {  // offsets of the problems' A entries in one concatenation
+        it.a_base = total_a;
+        total_a += it.a_nnz;
+    }
     {
         void *p = nullptr;
         cudaError_t e = cudaMalloc(&p, sizeof(Item) * std::max(count, 1));
@@ -219,8 +286,10 @@ extern "C" int ops_batch_create(ops_handle_t h, int dtype, int32_t count, const 
         void *f = nullptr;
         e = cudaMallocAsync(&f, sizeof(unsigned long long) * std::max(count, 1), st);
         if (e == cudaSuccess) e = cudaMemcpyAsync(b->d_items, b->items.data(), sizeof(Item) * count, cudaMemcpyHostToDevice, st);
-        if (e == cudaSuccess && count > 0) {
-            k_batch_flop<<<std::min(count, 65535), 256, 0, st>>>(b->d_items, count, static_cast<unsigned long long *>(f));
+        if (e == cudaSuccess) e = cudaMemsetAsync(f, 0, sizeof(unsigned long long) * std::max(count, 1), st);
+        if (e == cudaSuccess && count > 0 && total_a > 0) {
+            k_batch_flop<<<flat_grid(total_a, h->num_sms), 256, 0, st>>>(b->d_items, count, total_a,
+                                                                      static_cast<unsigned long long *>(f));
             e = cudaGetLastError();
         }
         if (e == cudaSuccess)
@@ -308,8 +377,14 @@ extern "C" int ops_batch_create(ops_handle_t h, int dtype, int32_t count, const 
         cudaError_t e = cudaMemcpyAsync(s.a_rpt + s.M, &last_a, sizeof(int), cudaMemcpyHostToDevice, st);
         if (e == cudaSuccess) e = cudaMemcpyAsync(s.b_rpt + s.K, &last_b, sizeof(int), cudaMemcpyHostToDevice, st);
         if (e == cudaSuccess && s.count > 0) {
-            k_batch_gather_structure<<<std::min(s.count, 65535), 256, 0, st>>>(b->d_items, s.first, s.count, s.a_rpt,
-                                                                              s.a_col, s.b_rpt, s.b_col);
+            const Item *its = b->d_items + s.first;
+            const int sms = h->num_sms;
+            if (s.M) k_batch_gather_field<kFARpt><<<flat_grid(s.M, sms), 256, 0, st>>>(its, s.count, s.M, s.a_rpt);
+            if (s.a_nnz)
+                k_batch_gather_field<kFACol><<<flat_grid(s.a_nnz, sms), 256, 0, st>>>(its, s.count, s.a_nnz, s.a_col);
+            if (s.K) k_batch_gather_field<kFBRpt><<<flat_grid(s.K, sms), 256, 0, st>>>(its, s.count, s.K, s.b_rpt);
+            if (s.b_nnz)
+                k_batch_gather_field<kFBCol><<<flat_grid(s.b_nnz, sms), 256, 0, st>>>(its, s.count, s.b_nnz, s.b_col);
             e = cudaGetLastError();
         }
         if (e == cudaSuccess) e = cudaStreamSynchronize(st);  // host values above must outlive the copies
@@ -352,12 +427,23 @@ int record_numeric(ops_batch_s *b, cudaStream_t st)
     ops_handle_s *h = b->owner;
     for (Segment &s : b->segs) {
         if (s.count == 0) continue;
-        if (b->dtype == OPS_F64)
-            k_batch_gather_values<double><<<std::min(s.count, 65535), 256, 0, st>>>(
-                b->d_items, s.first, s.count, static_cast<double *>(s.a_val), static_cast<double *>(s.b_val));
-        else
-            k_batch_gather_values<float><<<std::min(s.count, 65535), 256, 0, st>>>(
-                b->d_items, s.first, s.count, static_cast<float *>(s.a_val), static_cast<float *>(s.b_val));
+        const Item *its = b->d_items + s.first;
+        const int sms = h->num_sms;
+        if (b->dtype == OPS_F64) {
+            if (s.a_nnz)
+                k_batch_gather_vals<kFACol, double><<<flat_grid(s.a_nnz, sms), 256, 0, st>>>(
+                    its, s.count, s.a_nnz, static_cast<double *>(s.a_val));
+            if (s.b_nnz)
+                k_batch_gather_vals<kFBCol, double><<<flat_grid(s.b_nnz, sms), 256, 0, st>>>(
+                    its, s.count, s.b_nnz, static_cast<double *>(s.b_val));
+        } else {
+            if (s.a_nnz)
+                k_batch_gather_vals<kFACol, float><<<flat_grid(s.a_nnz, sms), 256, 0, st>>>(
+                    its, s.count, s.a_nnz, static_cast<float *>(s.a_val));
+            if (s.b_nnz)
+                k_batch_gather_vals<kFBCol, float><<<flat_grid(s.b_nnz, sms), 256, 0, st>>>(
+                    its, s.count, s.b_nnz, static_cast<float *>(s.b_val));
+        }
         OPS_CUDA(h, cudaGetLastError());
         const int stt = ops_spgemm_numeric(s.h, b->dtype, s.M, s.K, s.N, s.a_rpt, s.a_col, s.a_val, s.b_rpt, s.b_col,
                                            s.b_val, s.c_rpt, s.c_col, s.c_val, st);
