@@ -19,10 +19,10 @@ enum RowClass : int {
     kClsR8 = 0,   // flop <= 8,  lenA <= 8  : 8 lanes per row, registers only
     kClsR16 = 1,  // flop <= 16, lenA <= 16 : 16 lanes per row
     kClsR32 = 2,  // flop <= 32, lenA <= 32 : one warp per row
-    kClsW = 3,    // flop <= 128            : one warp per row, shared-memory hash table
-    kClsE1 = 4,   // flop <= 1024, lenA <= 1024   : 128-thread CTA per row, expand/sort/compress
-    kClsE2 = 5,   // flop <= 13312, lenA <= 2560  : 512-thread CTA per row, expand/sort/compress
-    kClsD = 6,    // larger                 : one CTA per row, dense accumulator in HBM
+    kClsW = 3,    // flop <= 128            : one warp per row, register sort
+    kClsE1 = 4,   // flop <= 1024, lenA <= 1024   : warp sort, warp hash or CTA bitonic sort
+    kClsE2 = 5,   // flop <= 13312, lenA <= 2560  : CTA bitonic sort (<= 4096) or CTA radix sort
+    kClsD = 6,    // larger                 : whole-GPU stable radix sort (dense accumulator fallback)
     kNumClasses = 7
 };
 
@@ -32,8 +32,7 @@ enum : int { kXlE1Sort = 0, kXlE1Hash = 1, kXlE1Esc = 2, kXlE2Mid = 3, kXlE2Larg
 constexpr int kNumLists = kNumClasses + kNumExtraLists;
 
 constexpr int kSmallFlopMax = 8;   // R8 rows: symbolic inside k_setup, numeric k_small_rows
-constexpr int kWarpFlopMax = 128;  // W rows: table of nextpow2(2*flop) <= 256 slots per warp
-constexpr int kWarpTableMax = 256;
+constexpr int kWarpFlopMax = 128;  // W rows: warp register sort of at most 128 products
 constexpr int kEsc1FlopMax = 1024;
 constexpr int kEsc1AMax = 1024;
 constexpr int kEsc2FlopMax = 13312;

@@ -1,6 +1,8 @@
-// esc.cuh — expand / sort / compress rows: one CTA per row for rows with 129..13312
-// intermediate products.  Replaces OpSparse's per-bin shared-hash kernels for its middle
-// and large bins (kernels/symbolic.cuh:74-261, kernels/numeric.cuh:109-302).
+// esc.cuh — expand / sort / compress rows, one CTA per row: the symbolic count of the E2
+// rows (hash table) and the numeric phase of the E2 rows above 4,096 products (radix
+// sort); also the device-side re-binning and ordering of class lists.  Replaces OpSparse's
+// per-bin shared-hash kernels for its large bins (kernels/symbolic.cuh:74-261,
+// kernels/numeric.cuh:109-302).
 //
 // Every thread of the CTA takes part in every step, so a row costs a few load-latency
 // levels instead of one dependent chain per warp:
@@ -47,7 +49,6 @@ struct EscShape {
     static constexpr size_t kSymbolicSmem = (size_t)kTable * 4 + (size_t)ACAP * 8 + 32 * 4 + 64;
 };
 
-using EscSmall = EscShape<128, 1024, 1024>;
 using EscMid = EscShape<256, 4096, 1280>;     // 75,968 B numeric: three CTAs per SM
 using EscLarge = EscShape<1024, 13312, 2560>;  // 223,424 B numeric: one 1024-thread CTA per SM
 

@@ -73,8 +73,6 @@ void launch_besc(const SpgemmArgs<T> &g, const int *list, const int *count_ptr, 
 template <typename T>
 void set_smem_attrs()
 {
-    cudaFuncSetAttribute(k_warp_rows<true, T, kWarpTableMax>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)warp_rows_smem<true, T, kWarpTableMax>());
     cudaFuncSetAttribute(k_warp_rows<true, T, 2 * kSplitNnz>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)warp_rows_smem<true, T, 2 * kSplitNnz>());
     cudaFuncSetAttribute(k_esc_rows<EscLarge, true, T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
