@@ -46,6 +46,7 @@ struct EscShape {
     static constexpr size_t kNumericSmem = (size_t)PCAP * (4 + 4 + 2 + 2 + 2) + (size_t)kWarps * kDigits * 2 +
                                            (size_t)ACAP * 8 + 32 * 4 + 64;
     static_assert(PCAP < 65536, "16-bit radix offsets");
+    static_assert(PCAP / 16 < NT / 32 * 128, "long-run list fits the histogram space");
     static constexpr size_t kSymbolicSmem = (size_t)kTable * 4 + (size_t)ACAP * 8 + 32 * 4 + 64;
 };
 
@@ -53,6 +54,7 @@ using EscMid = EscShape<256, 4096, 1280>;     // 75,968 B numeric: three CTAs pe
 using EscLarge = EscShape<1024, 13312, 2560>;  // 223,424 B numeric: one 1024-thread CTA per SM
 
 constexpr int kUnroll = 4;  // chunks (expansion) or products (fold) with loads in flight together
+constexpr int kLongRun = 16;  // numeric: runs of this many products or more are folded by a warp
 
 // Smallest t in [0, n) with incl[t] > p (incl non-decreasing, incl[n-1] > p).
 __device__ __forceinline__ int esc_owner(const int *incl, int n, int p)
@@ -141,7 +143,7 @@ __device__ __forceinline__ int esc_scan_row(const SpgemmArgs<T> &g, int a0, int 
 }
 
 template <typename Shape, bool kNum, typename T>
-__global__ void __launch_bounds__(Shape::kThreads) k_esc_rows(SpgemmArgs<T> g, const int *__restrict__ list,
+__global__ void __launch_bounds__(Shape::kThreads, 1) k_esc_rows(SpgemmArgs<T> g, const int *__restrict__ list,
                                                               const int *count_ptr, int *cursor)
 {
     using AccT = Acc<T>;
@@ -284,15 +286,15 @@ __global__ void __launch_bounds__(Shape::kThreads) k_esc_rows(SpgemmArgs<T> g, c
             unsigned short *wh = hist + warp * Shape::kDigits;
             for (int pass = 0; pass < passes; ++pass) {
                 const int shift = 8 * pass;
-                for (int d = lane; d < Shape::kDigits; d += 32) wh[d] = 0;
+                const int nbits = min(8, key_bits - shift);
+                // the warp's 16-bit counters, two to a word, counted with shared-memory
+                // atomics (order-free; a slice holds fewer than 2^16 elements)
+                unsigned *wh32 = reinterpret_cast<unsigned *>(wh);
+                for (int d = lane; d < Shape::kDigits / 2; d += 32) wh32[d] = 0u;
                 __syncwarp();
-                for (int c = rb; c < re; c += 32) {
-                    const int i = c + lane;
-                    const bool valid = i < re;
-                    const int d = valid ? (int)((kin[i] >> shift) & 255u) : 256 + lane;
-                    const unsigned peers = __match_any_sync(kFull, d);
-                    if (valid && lane == __ffs(peers) - 1) wh[d] += __popc(peers);
-                    __syncwarp();
+                for (int i = rb + lane; i < re; i += 32) {
+                    const unsigned d = (kin[i] >> shift) & 255u;
+                    atomicAdd(&wh32[d >> 1], 1u << ((d & 1u) * 16));
                 }
                 __syncthreads();
                 // exclusive offsets in (digit, warp) order: element i of the scan is
@@ -322,8 +324,17 @@ __global__ void __launch_bounds__(Shape::kThreads) k_esc_rows(SpgemmArgs<T> g, c
                     const bool valid = i < re;
                     const unsigned key = valid ? kin[i] : 0u;
                     const unsigned short id = valid ? iin[i] : (unsigned short)0;
-                    const int d = valid ? (int)((key >> shift) & 255u) : 256 + lane;
-                    const unsigned peers = __match_any_sync(kFull, d);
+                    const int d = (int)((key >> shift) & 255u);
+                    // lanes holding the same digit: one ballot per digit bit
+                    unsigned peers = c + 32 <= re ? kFull : __ballot_sync(kFull, valid);
+#pragma unroll
+                    for (int b = 0; b < 8; ++b) {
+                        if (b < nbits) {
+                            const bool bit = (d >> b) & 1;
+                            const unsigned m = __ballot_sync(kFull, bit);
+                            peers &= bit ? m : ~m;
+                        }
+                    }
                     const int leader = __ffs(peers) - 1;
                     int base = 0;
                     if (lane == leader && valid) base = wh[d];
@@ -351,23 +362,70 @@ __global__ void __launch_bounds__(Shape::kThreads) k_esc_rows(SpgemmArgs<T> g, c
             const int ie = min(n, ib + E);
             int heads = 0;
             for (int i = ib; i < ie; ++i) heads += (i == 0 || kin[i] != kin[i - 1]) ? 1 : 0;
+            if (tid == 0) s_count = 0;
             int total = 0;
             const int hincl = block_inclusive_scan(heads, s_warp_sums, &total);
             if (tid == 0 && total != n_expect) atomicOr(&g.info->flags, kErrCountMismatch);
-            // output position of every run head, kept in the free ping-pong key buffer
+            // output position of every run head, kept in the free ping-pong key buffer;
+            // runs of kLongRun or more products are listed (in the histogram space, free
+            // after the sort) for the warp-per-run fold below
             unsigned *hpos = kout;
+            int *long_runs = reinterpret_cast<int *>(hist);
             int pos = hincl - heads;
-            for (int i = ib; i < ie; ++i)
-                if (i == 0 || kin[i] != kin[i - 1]) hpos[i] = (unsigned)pos++;
+            for (int i = ib; i < ie; ++i) {
+                if (i == 0 || kin[i] != kin[i - 1]) {
+                    hpos[i] = (unsigned)pos++;
+                    if (i + kLongRun <= n && kin[i + kLongRun - 1] == kin[i]) long_runs[atomicAdd(&s_count, 1)] = i;
+                }
+            }
             __syncthreads();
-            // heads are processed thread-strided, so neighbouring threads work on
-            // neighbouring runs and their loads and C stores coalesce
-            // A run is folded kUnroll products at a time: the operands of a batch are
-            // all loaded before its first FMA, so a run of length L waits on memory
-            // ceil(L / kUnroll) times rather than L times.
+            // product t's operands (t a sorted position)
+            auto operands = [&](int t, T &a, T &b) {
+                const int q = iin[t];
+                const int o = own[q];
+                const int k = s_b0[o] + q - (o ? s_incl[o - 1] : 0);
+                a = __ldg(g.aval + a0 + o);
+                b = __ldg(g.bval + k);
+            };
+            // long runs: one warp each.  The lanes load the operands of the next 32
+            // products while the fold of the current 32 runs; lane 0 folds them in order
+            // from shuffles, so the run costs about one FMA latency per product.
+            const int n_long = s_count;
+            for (int w = warp; w < n_long; w += NW) {
+                const int i0 = long_runs[w];
+                const unsigned key = kin[i0];
+                T a = T(0), b = T(0);
+                if (i0 + lane < n && kin[i0 + lane] == key) operands(i0 + lane, a, b);
+                S s = AccT::zero();
+                for (int t = i0;; t += 32) {
+                    const int tn = t + 32 + lane;
+                    const unsigned vm = __ballot_sync(kFull, t + lane < n && kin[t + lane] == key);
+                    T na = T(0), nb = T(0);
+                    if (vm == kFull && tn < n && kin[tn] == key) operands(tn, na, nb);
+                    const int m = __popc(vm);  // the run is contiguous: lanes [0, m)
+#pragma unroll
+                    for (int u = 0; u < 32; ++u) {
+                        const T au = shfl(a, u), bu = shfl(b, u);
+                        if (lane == 0 && u < m) s = AccT::step(s, au, bu);
+                    }
+                    if (vm != kFull) break;
+                    a = na;
+                    b = nb;
+                }
+                const int hp = (int)hpos[i0];
+                if (lane == 0 && hp < n_expect) {
+                    g.c_col[off + hp] = (int)key;
+                    g.c_val[off + hp] = AccT::fin(s);
+                }
+            }
+            // short runs: heads are processed thread-strided, so neighbouring threads work
+            // on neighbouring runs and their loads and C stores coalesce.  A run is folded
+            // kUnroll products at a time: the operands of a batch are all loaded before
+            // its first FMA, so a run of length L waits on memory ceil(L / kUnroll) times.
             for (int i = tid; i < n; i += NT) {
                 const unsigned key = kin[i];
                 if (i > 0 && kin[i - 1] == key) continue;
+                if (i + kLongRun <= n && kin[i + kLongRun - 1] == key) continue;
                 S s = AccT::zero();
                 bool more = true;
                 for (int t = i; more; t += kUnroll) {
@@ -381,13 +439,7 @@ __global__ void __launch_bounds__(Shape::kThreads) k_esc_rows(SpgemmArgs<T> g, c
                         v[u] = run;
                         av[u] = T(0);
                         bv[u] = T(0);
-                        if (run) {
-                            const int q = iin[tt];
-                            const int o = own[q];
-                            const int k = s_b0[o] + q - (o ? s_incl[o - 1] : 0);
-                            av[u] = __ldg(g.aval + a0 + o);
-                            bv[u] = __ldg(g.bval + k);
-                        }
+                        if (run) operands(tt, av[u], bv[u]);
                     }
 #pragma unroll
                     for (int u = 0; u < kUnroll; ++u)
