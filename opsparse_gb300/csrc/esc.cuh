@@ -356,7 +356,9 @@ __global__ void __launch_bounds__(Shape::kThreads, 1) k_esc_rows(SpgemmArgs<T> g
                 iin = iout;
                 iout = ti;
             }
-            // run heads -> output positions (contiguous element ranges per thread)
+            // run heads: thread tid owns positions [ib, ie) and the runs whose head lies
+            // there; hidx[h] = position of head h, which is also C entry h of the row
+            // (kept in the free ping-pong key buffer)
             const int E = (n + NT - 1) / NT;
             const int ib = min(n, tid * E);
             const int ie = min(n, ib + E);
@@ -366,18 +368,17 @@ __global__ void __launch_bounds__(Shape::kThreads, 1) k_esc_rows(SpgemmArgs<T> g
             int total = 0;
             const int hincl = block_inclusive_scan(heads, s_warp_sums, &total);
             if (tid == 0 && total != n_expect) atomicOr(&g.info->flags, kErrCountMismatch);
-            // output position of every run head, kept in the free ping-pong key buffer;
+            int *hidx = reinterpret_cast<int *>(kout);
+            const int hs = hincl - heads, he = hincl;
+            for (int i = ib, h = hs; i < ie; ++i)
+                if (i == 0 || kin[i] != kin[i - 1]) hidx[h++] = i;
+            __syncthreads();
+            auto run_end = [&](int h) { return h + 1 < total ? hidx[h + 1] : n; };
             // runs of kLongRun or more products are listed (in the histogram space, free
-            // after the sort) for the warp-per-run fold below
-            unsigned *hpos = kout;
+            // after the sort) for the warp-per-run fold
             int *long_runs = reinterpret_cast<int *>(hist);
-            int pos = hincl - heads;
-            for (int i = ib; i < ie; ++i) {
-                if (i == 0 || kin[i] != kin[i - 1]) {
-                    hpos[i] = (unsigned)pos++;
-                    if (i + kLongRun <= n && kin[i + kLongRun - 1] == kin[i]) long_runs[atomicAdd(&s_count, 1)] = i;
-                }
-            }
+            for (int h = hs; h < he; ++h)
+                if (run_end(h) - hidx[h] >= kLongRun) long_runs[atomicAdd(&s_count, 1)] = h;
             __syncthreads();
             // product t's operands (t a sorted position)
             auto operands = [&](int t, T &a, T &b) {
@@ -387,69 +388,82 @@ __global__ void __launch_bounds__(Shape::kThreads, 1) k_esc_rows(SpgemmArgs<T> g
                 a = __ldg(g.aval + a0 + o);
                 b = __ldg(g.bval + k);
             };
+            auto write_c = [&](int h, int t, S s) {
+                if (h < n_expect) {
+                    g.c_col[off + h] = (int)kin[t];
+                    g.c_val[off + h] = AccT::fin(s);
+                }
+            };
             // long runs: one warp each.  The lanes load the operands of the next 32
             // products while the fold of the current 32 runs; lane 0 folds them in order
             // from shuffles, so the run costs about one FMA latency per product.
             const int n_long = s_count;
             for (int w = warp; w < n_long; w += NW) {
-                const int i0 = long_runs[w];
-                const unsigned key = kin[i0];
+                const int h = long_runs[w];
+                const int i0 = hidx[h], i1 = run_end(h);
                 T a = T(0), b = T(0);
-                if (i0 + lane < n && kin[i0 + lane] == key) operands(i0 + lane, a, b);
+                if (i0 + lane < i1) operands(i0 + lane, a, b);
                 S s = AccT::zero();
-                for (int t = i0;; t += 32) {
-                    const int tn = t + 32 + lane;
-                    const unsigned vm = __ballot_sync(kFull, t + lane < n && kin[t + lane] == key);
+                for (int t = i0; t < i1; t += 32) {
                     T na = T(0), nb = T(0);
-                    if (vm == kFull && tn < n && kin[tn] == key) operands(tn, na, nb);
-                    const int m = __popc(vm);  // the run is contiguous: lanes [0, m)
+                    if (t + 32 + lane < i1) operands(t + 32 + lane, na, nb);
+                    const int m = min(32, i1 - t);
 #pragma unroll
                     for (int u = 0; u < 32; ++u) {
                         const T au = shfl(a, u), bu = shfl(b, u);
                         if (lane == 0 && u < m) s = AccT::step(s, au, bu);
                     }
-                    if (vm != kFull) break;
                     a = na;
                     b = nb;
                 }
-                const int hp = (int)hpos[i0];
-                if (lane == 0 && hp < n_expect) {
-                    g.c_col[off + hp] = (int)key;
-                    g.c_val[off + hp] = AccT::fin(s);
-                }
+                if (lane == 0) write_c(h, i0, s);
             }
-            // short runs: heads are processed thread-strided, so neighbouring threads work
-            // on neighbouring runs and their loads and C stores coalesce.  A run is folded
-            // kUnroll products at a time: the operands of a batch are all loaded before
-            // its first FMA, so a run of length L waits on memory ceil(L / kUnroll) times.
-            for (int i = tid; i < n; i += NT) {
-                const unsigned key = kin[i];
-                if (i > 0 && kin[i - 1] == key) continue;
-                if (i + kLongRun <= n && kin[i + kLongRun - 1] == key) continue;
+            // short runs: each thread walks the concatenation of its own runs (long ones
+            // skipped) one product per step, the operands of kUnroll steps loaded
+            // together.  A warp-wide FP64 FMA costs the same however few lanes are
+            // active, so the steps are packed: a warp issues about as many FMAs as its
+            // busiest lane has products.
+            {
+                int h = hs, t = 0, e = 0;  // current run, next position, end of the run
+                auto next_short = [&]() {   // from run h on: the first short run, or h == he
+                    for (; h < he; ++h) {
+                        t = hidx[h];
+                        e = run_end(h);
+                        if (e - t < kLongRun) return;
+                    }
+                };
+                next_short();
                 S s = AccT::zero();
-                bool more = true;
-                for (int t = i; more; t += kUnroll) {
+                while (h < he) {
                     T av[kUnroll], bv[kUnroll];
-                    bool v[kUnroll];
-                    bool run = true;
+                    int hu[kUnroll], pu[kUnroll];
 #pragma unroll
                     for (int u = 0; u < kUnroll; ++u) {
-                        const int tt = t + u;
-                        run = run && tt < n && kin[tt] == key;
-                        v[u] = run;
+                        hu[u] = -1;
+                        pu[u] = 0;
                         av[u] = T(0);
                         bv[u] = T(0);
-                        if (run) operands(tt, av[u], bv[u]);
+                        if (h < he) {
+                            hu[u] = h;
+                            pu[u] = t;
+                            operands(t, av[u], bv[u]);
+                            if (++t == e) {
+                                ++h;
+                                next_short();
+                            }
+                        }
                     }
 #pragma unroll
-                    for (int u = 0; u < kUnroll; ++u)
-                        if (v[u]) s = AccT::step(s, av[u], bv[u]);
-                    more = v[kUnroll - 1];
-                }
-                const int hp = (int)hpos[i];
-                if (hp < n_expect) {
-                    g.c_col[off + hp] = (int)key;
-                    g.c_val[off + hp] = AccT::fin(s);
+                    for (int u = 0; u < kUnroll; ++u) {
+                        if (hu[u] >= 0) {
+                            s = AccT::step(s, av[u], bv[u]);
+                            const int hn = u + 1 < kUnroll ? hu[u + 1] : (h < he ? h : -1);
+                            if (hn != hu[u]) {  // run hu[u] is complete
+                                write_c(hu[u], pu[u], s);
+                                s = AccT::zero();
+                            }
+                        }
+                    }
                 }
             }
             __syncthreads();

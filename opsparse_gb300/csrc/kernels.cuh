@@ -349,8 +349,8 @@ __global__ void __launch_bounds__(kSmallThreads, 4) k_small_rows(SpgemmArgs<T> g
 
 // ==================================================================================
 // R classes: G lanes per row (G = 8, 16, 32), all of the row's products in one chunk.
-// Lane q of a group holds product q; duplicates are found by comparing every pair of
-// the group's lanes through shuffles, the lowest lane of each column is its leader.  Symbolic: nnz = number of leaders.
+// Lane q of a group holds product q; duplicates are found with __match_any_sync, the
+// lowest lane of each match group is its leader.  Symbolic: nnz = number of leaders.
 // Numeric: each leader folds its group in lane order (= ascending j), ranks itself
 // among the group's leaders by column, and writes C directly in sorted position.
 // Grid-stride over the class list; every lane of a warp runs the same trip count.
@@ -404,19 +404,8 @@ __global__ void __launch_bounds__(256) k_reg_rows(SpgemmArgs<T> g, const int *__
         const int o_b0 = __shfl_sync(kFull, b0, lo, G);
         const int k = o_b0 + (q - (o_incl - o_bl));
         const int col = valid ? __ldg(g.bcol + k) : kEmpty;
-        // duplicates by comparing with every lane of the group (a match instruction costs
-        // more issue slots on this GPU): eq / less = the group's lanes holding the same /
-        // a smaller column, as group-relative lane masks
-        unsigned eq = 0u, less = 0u;
-#pragma unroll
-        for (int t = 0; t < G; ++t) {
-            const int ct = __shfl_sync(kFull, col, t, G);
-            const bool in = t < flop;
-            eq |= (in && ct == col) ? (1u << t) : 0u;
-            if constexpr (kNum) less |= (in && ct < col) ? (1u << t) : 0u;
-        }
-        const bool leader = valid && (eq & ((1u << q) - 1u)) == 0u;
-        const int gbase = lane & ~(G - 1);
+        const unsigned m = __match_any_sync(kFull, col) & gmask;
+        const bool leader = valid && (lane == __ffs(m) - 1);
 
         if constexpr (!kNum) {
             const unsigned lb = __ballot_sync(kFull, leader) & gmask;
@@ -425,12 +414,16 @@ __global__ void __launch_bounds__(256) k_reg_rows(SpgemmArgs<T> g, const int *__
                 nnz_acc += (unsigned long long)__popc(lb);
             }
         } else {
-            const T o_av = shfl(av, lo + gbase);
+            const T o_av = shfl(av, lo + (lane & ~(G - 1)));
             const T bv = valid ? __ldg(g.bval + k) : T(0);
-            S s = fold_group<T>(AccT::zero(), leader ? (eq << gbase) : 0u, o_av, bv);
-            // rank among the group's distinct columns = smaller columns held by leaders
-            const unsigned lrel = (__ballot_sync(kFull, leader) & gmask) >> gbase;
-            const int rank = __popc(less & lrel);
+            S s = fold_group<T>(AccT::zero(), leader ? m : 0u, o_av, bv);
+            int rank = 0;
+#pragma unroll
+            for (int t = 0; t < G; ++t) {
+                const int ct = __shfl_sync(kFull, col, t, G);
+                const int lt = __shfl_sync(kFull, (int)leader, t, G);
+                rank += (lt && ct < col) ? 1 : 0;
+            }
             if (leader) {
                 const int pos = __ldg(g.c_rpt + r) + rank;
                 g.c_col[pos] = col;
@@ -672,10 +665,8 @@ __global__ void __launch_bounds__(kWarpRowsThreads) k_warp_rows(SpgemmArgs<T> g,
         } else
         warp_products<kNum, T>(a0, a1, 32, g.acol, g.aval, g.brpt, [&](bool valid, int k, T av, int) {
             const int col = valid ? __ldg(g.bcol + k) : kEmpty;
-            unsigned m = 0u;  // lanes holding the same column (pairwise, through shuffles)
-#pragma unroll
-            for (int t = 0; t < 32; ++t) m |= (__shfl_sync(kFull, col, t) == col) ? (1u << t) : 0u;
-            const bool leader = valid && (m & lanemask_lt()) == 0u;
+            const unsigned m = __match_any_sync(kFull, col);
+            const bool leader = valid && (lane == __ffs(m) - 1);
             int slot = -1;
             if (leader) {
                 bool is_new = false;
