@@ -92,6 +92,11 @@ struct SpgemmArgs {
     int *c_col;
     T *c_val;
     DevInfo *info;
+    // One-pass numeric (register and W rows, run inside the counting phase): when > 0,
+    // the row at list index i writes its entries to c_col/c_val + i * stage_cap (a
+    // staging area), its count to c_rpt[r] and the count to info->total_nnz, as the
+    // counting kernels do; k_place_staged moves the entries to C after the scan.
+    int stage_cap;
 };
 
 __device__ __forceinline__ int lane_id() { return threadIdx.x & 31; }

@@ -418,54 +418,11 @@ __global__ void __launch_bounds__(Shape::kThreads, 1) k_esc_rows(SpgemmArgs<T> g
                 }
                 if (lane == 0) write_c(h, i0, s);
             }
-            // short runs: each thread walks the concatenation of its own runs (long ones
-            // skipped) one product per step, the operands of kUnroll steps loaded
-            // together.  A warp-wide FP64 FMA costs the same however few lanes are
-            // active, so the steps are packed: a warp issues about as many FMAs as its
-            // busiest lane has products.
-            {
-                int h = hs, t = 0, e = 0;  // current run, next position, end of the run
-                auto next_short = [&]() {   // from run h on: the first short run, or h == he
-                    for (; h < he; ++h) {
-                        t = hidx[h];
-                        e = run_end(h);
-                        if (e - t < kLongRun) return;
-                    }
-                };
-                next_short();
-                S s = AccT::zero();
-                while (h < he) {
-                    T av[kUnroll], bv[kUnroll];
-                    int hu[kUnroll], pu[kUnroll];
-#pragma unroll
-                    for (int u = 0; u < kUnroll; ++u) {
-                        hu[u] = -1;
-                        pu[u] = 0;
-                        av[u] = T(0);
-                        bv[u] = T(0);
-                        if (h < he) {
-                            hu[u] = h;
-                            pu[u] = t;
-                            operands(t, av[u], bv[u]);
-                            if (++t == e) {
-                                ++h;
-                                next_short();
-                            }
-                        }
-                    }
-#pragma unroll
-                    for (int u = 0; u < kUnroll; ++u) {
-                        if (hu[u] >= 0) {
-                            s = AccT::step(s, av[u], bv[u]);
-                            const int hn = u + 1 < kUnroll ? hu[u + 1] : (h < he ? h : -1);
-                            if (hn != hu[u]) {  // run hu[u] is complete
-                                write_c(hu[u], pu[u], s);
-                                s = AccT::zero();
-                            }
-                        }
-                    }
-                }
-            }
+            // short runs: this thread's own runs, packed steps (long ones skipped)
+            fold_own_runs<T>(
+                hs, he, kLongRun, [&](int h) { return hidx[h]; }, run_end,
+                [&](int t, T &a, T &b, int &) { operands(t, a, b); },
+                [&](int h, int t, int, S s) { write_c(h, t, s); });
             __syncthreads();
         }
     }

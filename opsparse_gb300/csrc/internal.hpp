@@ -67,6 +67,18 @@ struct ops_handle_s {
     size_t dense_bytes = 0;
     int dense_ctas = 0;
 
+    // one-pass numeric of the R16, R32 and W rows (ops_spgemm, where the values are known
+    // before the counting phase): their numeric kernels run in the counting phase into a
+    // staging area (grow-only) and are placed into C after the scan
+    bool one_pass = true;          // allowed on this handle
+    int op_dtype = -1;             // value type of the call in progress, -1 = two passes
+    const void *op_aval = nullptr, *op_bval = nullptr;
+    bool staged = false;           // the counting phase just staged those classes
+    unsigned char *stage = nullptr;
+    size_t stage_bytes = 0;
+    size_t stage_budget = size_t(2) << 30;  // larger staging areas fall back to two passes
+    size_t stage_off[kNumClasses] = {};  // byte offsets of a class's [columns | values]
+
     // plan of the last symbolic phase
     bool plan_valid = false;
     int plan_M = 0, plan_K = 0, plan_N = 0;

@@ -52,6 +52,66 @@ __device__ __forceinline__ void block_add_u64(unsigned long long v, unsigned lon
     __syncthreads();
 }
 
+constexpr int kFoldUnroll = 4;  // fold steps whose operands are loaded together
+
+// Folds the runs [hs, he) owned by the calling thread (run h covers the sorted positions
+// [head(h), end(h)); runs of skip_len or more products are left to the caller): the
+// concatenation of the runs is walked one product per step, the operands of kFoldUnroll
+// steps loaded together (load(t, a, b, k) gives product t's operands and its B index),
+// and each completed run is passed to write(h, t, k, s) with one of its positions and B
+// indices.  A warp-wide FP64 FMA costs the same however few lanes are active, so packing
+// the steps makes a warp issue about as many FMAs as its busiest lane has products,
+// where one run per lane per step would issue kFoldUnroll per run.
+template <typename T, typename Head, typename End, typename Load, typename Write>
+__device__ __forceinline__ void fold_own_runs(int hs, int he, int skip_len, Head head, End end, Load load,
+                                              Write write)
+{
+    using AccT = Acc<T>;
+    using S = typename AccT::S;
+    int h = hs, t = 0, e = 0;  // current run, next position, end of the run
+    auto next_run = [&]() {    // from run h on: the first run to fold, or h == he
+        for (; h < he; ++h) {
+            t = head(h);
+            e = end(h);
+            if (e - t < skip_len) return;
+        }
+    };
+    next_run();
+    S s = AccT::zero();
+    while (h < he) {
+        T av[kFoldUnroll], bv[kFoldUnroll];
+        int hu[kFoldUnroll], pu[kFoldUnroll], ku[kFoldUnroll];
+#pragma unroll
+        for (int u = 0; u < kFoldUnroll; ++u) {
+            hu[u] = -1;
+            pu[u] = 0;
+            ku[u] = 0;
+            av[u] = T(0);
+            bv[u] = T(0);
+            if (h < he) {
+                hu[u] = h;
+                pu[u] = t;
+                load(t, av[u], bv[u], ku[u]);
+                if (++t == e) {
+                    ++h;
+                    next_run();
+                }
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < kFoldUnroll; ++u) {
+            if (hu[u] >= 0) {
+                s = AccT::step(s, av[u], bv[u]);
+                const int hn = u + 1 < kFoldUnroll ? hu[u + 1] : (h < he ? h : -1);
+                if (hn != hu[u]) {  // run hu[u] is complete
+                    write(hu[u], pu[u], ku[u], s);
+                    s = AccT::zero();
+                }
+            }
+        }
+    }
+}
+
 // ==================================================================================
 // Setup: per-row product count, validation of A's columns, class assignment, and the
 // scatter of row ids into per-class lists (lists[c * M + i]).  One thread per row for
@@ -424,14 +484,47 @@ __global__ void __launch_bounds__(256) k_reg_rows(SpgemmArgs<T> g, const int *__
                 const int lt = __shfl_sync(kFull, (int)leader, t, G);
                 rank += (lt && ct < col) ? 1 : 0;
             }
-            if (leader) {
+            if (g.stage_cap) {  // one-pass: staging slot of the list entry, count as symbolic
+                if (leader) {
+                    const long long pos = gid * g.stage_cap + rank;
+                    g.c_col[pos] = col;
+                    g.c_val[pos] = AccT::fin(s);
+                }
+                const unsigned lb = __ballot_sync(kFull, leader) & gmask;
+                if (active && q == 0) {
+                    g.c_rpt[r] = __popc(lb);
+                    nnz_acc += (unsigned long long)__popc(lb);
+                }
+            } else if (leader) {
                 const int pos = __ldg(g.c_rpt + r) + rank;
                 g.c_col[pos] = col;
                 g.c_val[pos] = AccT::fin(s);
             }
         }
     }
-    if constexpr (!kNum) warp_add_u64(nnz_acc, &g.info->total_nnz);
+    if (!kNum || g.stage_cap) warp_add_u64(nnz_acc, &g.info->total_nnz);
+}
+
+// Moves staged rows (one-pass numeric) into C: list entry i's slot at i << log_cap holds
+// the row's c_rpt[r+1] - c_rpt[r] entries.  One thread per slot, so the staging area is
+// read and C written in order.
+template <typename T>
+__global__ void k_place_staged(const int *__restrict__ list, int count, int log_cap, const int *__restrict__ scol,
+                               const T *__restrict__ sval, const int *__restrict__ c_rpt, int *__restrict__ c_col,
+                               T *__restrict__ c_val)
+{
+    const long long total = (long long)count << log_cap;
+    const int mask = (1 << log_cap) - 1;
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < total;
+         t += (long long)gridDim.x * blockDim.x) {
+        const int r = __ldg(list + (t >> log_cap));
+        const int e = (int)t & mask;
+        const int o = __ldg(c_rpt + r);
+        if (e < __ldg(c_rpt + r + 1) - o) {
+            c_col[o + e] = scol[t];
+            c_val[o + e] = sval[t];
+        }
+    }
 }
 
 // ==================================================================================

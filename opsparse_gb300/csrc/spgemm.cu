@@ -166,6 +166,88 @@ int grid_for(long long work_items, int per_block, int cap)
     return (int)std::max<long long>(1, std::min<long long>(b, cap));
 }
 
+// Staging capacity (entries per row) of the classes with a one-pass numeric.
+constexpr int stage_cap_of(int c) { return c == kClsR16 ? 16 : c == kClsR32 ? 32 : c == kClsW ? kWarpFlopMax : 0; }
+
+template <typename T>
+T *stage_vals(ops_handle_s *h, int c, int n)
+{
+    return reinterpret_cast<T *>(h->stage + h->stage_off[c] + align_up(sizeof(int) * (size_t)n * stage_cap_of(c), 256));
+}
+
+// Counting phase of a one-pass call: class c's numeric kernel writes the rows' entries
+// to the staging area and their counts to c_rpt, in place of the counting kernel.
+template <typename T, typename GA>
+void launch_staged_numeric(ops_handle_s *h, const GA &gs, int c, const int *list, int n, cudaStream_t s)
+{
+    SpgemmArgs<T> g{};
+    g.arpt = gs.arpt;
+    g.acol = gs.acol;
+    g.aval = static_cast<const T *>(h->op_aval);
+    g.brpt = gs.brpt;
+    g.bcol = gs.bcol;
+    g.bval = static_cast<const T *>(h->op_bval);
+    g.M = gs.M;
+    g.K = gs.K;
+    g.N = gs.N;
+    g.row_flop = gs.row_flop;
+    g.c_rpt = gs.c_rpt;
+    g.info = gs.info;
+    g.stage_cap = stage_cap_of(c);
+    g.c_col = reinterpret_cast<int *>(h->stage + h->stage_off[c]);
+    g.c_val = stage_vals<T>(h, c, n);
+    const int sms = h->num_sms;
+    if (c == kClsR16) {
+        k_reg_rows<16, true, T><<<grid_for((n + 1) / 2, 8, sms * 8), 256, 0, s>>>(g, list, n);
+    } else if (c == kClsR32) {
+        k_reg_rows<32, true, T><<<grid_for(n, 8, sms * 8), 256, 0, s>>>(g, list, n);
+    } else {
+        using Sh = WsortShape<4>;
+        const int grid = grid_for(n, Sh::kWarps, sms * 8);
+        if (g.N <= (1 << (32 - Sh::kIdBits))) {
+            k_wsort_rows<4, true, T, unsigned>
+                <<<grid, Sh::kThreads, Sh::smem<true, T, unsigned>(), s>>>(g, list, &h->info->counts[c]);
+        } else {
+            k_wsort_rows<4, true, T, unsigned long long>
+                <<<grid, Sh::kThreads, Sh::smem<true, T, unsigned long long>(), s>>>(g, list, &h->info->counts[c]);
+        }
+    }
+}
+
+// One-pass set-up, once the class sizes are known: lays out (and grows) the staging area
+// of the R16, R32 and W rows.  Leaves h->staged false — two passes — when the call has no
+// values yet, one-pass is off, no row is in those classes, or the area would exceed the
+// handle's staging budget.
+int prepare_stage(ops_handle_s *h, cudaStream_t st)
+{
+    h->staged = false;
+    const int vs = h->op_dtype == OPS_F64 ? 8 : (h->op_dtype == OPS_F32 ? 4 : 0);
+    if (!h->one_pass || vs == 0) return OPS_OK;
+    size_t total = 0;
+    int rows = 0;
+    for (int c = 0; c < kNumClasses; ++c) {
+        const size_t slots = (size_t)h->counts[c] * (size_t)stage_cap_of(c);
+        h->stage_off[c] = total;
+        total += align_up(sizeof(int) * slots, 256) + align_up((size_t)vs * slots, 256);
+        if (stage_cap_of(c)) rows += h->counts[c];
+    }
+    if (rows == 0 || total > h->stage_budget) return OPS_OK;
+    if (total > h->stage_bytes) {
+        if (h->stage) OPS_CUDA(h, cudaFreeAsync(h->stage, st));
+        h->stage = nullptr;
+        h->stage_bytes = 0;
+        void *p = nullptr;
+        if (cudaMallocFromPoolAsync(&p, total, h->pool, st) != cudaSuccess) {  // two passes instead
+            (void)cudaGetLastError();
+            return OPS_OK;
+        }
+        h->stage = static_cast<unsigned char *>(p);
+        h->stage_bytes = total;
+    }
+    h->staged = true;
+    return OPS_OK;
+}
+
 // Launch the kernels of every non-empty class, each on its own stream forked from `st`
 // and joined back into it.  A re-binned class (E1 numeric, E2) first splits its list on
 // the device and runs its second kernel on an extra stream forked from the class stream;
@@ -204,6 +286,16 @@ int launch_classes(ops_handle_s *h, const SpgemmArgs<T> &g, cudaStream_t st)
             ++h->launches;
         }
         if (h->timing >= 2) OPS_CUDA(h, cudaEventRecord(h->ev_k[kNum][c][0], s));
+        const bool staged = h->staged && stage_cap_of(c) > 0;
+        if (staged && !kNum) {  // one-pass call: numeric into the staging area
+            if (h->op_dtype == OPS_F64) launch_staged_numeric<double>(h, g, c, list, n, s);
+            else launch_staged_numeric<float>(h, g, c, list, n, s);
+        } else if (staged) {    // ... and its placement into C
+            const int cap = stage_cap_of(c);
+            k_place_staged<T><<<grid_for((long long)n * cap, 256, sms * 8), 256, 0, s>>>(
+                list, n, ceil_log2(cap), reinterpret_cast<const int *>(h->stage + h->stage_off[c]),
+                stage_vals<T>(h, c, n), g.c_rpt, g.c_col, g.c_val);
+        } else
         switch (c) {
             case kClsR8:  // numeric only: walks the rows in order
                 k_small_rows<T><<<grid_for(g.M, kSmallThreads, sms * 8), kSmallThreads, 0, s>>>(g, h->plan_th.r8);
@@ -391,6 +483,7 @@ int run_symbolic(ops_handle_s *h, const Mat &A, const Mat &B, int *c_rpt, long l
     h->plan_flop = (long long)hi.total_flop;
     h->plan_d_flop = (long long)hi.d_flop;
     h->plan_d_len_a = (long long)hi.d_len_a;
+    OPS_CHECK(prepare_stage(h, st));
 
     SpgemmArgs<double> g{};
     g.arpt = A.rpt;
@@ -588,6 +681,7 @@ int ops_handle_destroy(ops_handle_t h)
     cudaDeviceSynchronize();
     if (h->ws) cudaFree(h->ws);
     if (h->dense) cudaFree(h->dense);
+    if (h->stage) cudaFree(h->stage);
     for (int c = 0; c < kNumClasses; ++c) {
         if (h->side[c]) cudaStreamDestroy(h->side[c]);
         if (h->ev_join[c]) cudaEventDestroy(h->ev_join[c]);
@@ -654,6 +748,13 @@ int ops_handle_get_thresholds(ops_handle_t h, int32_t *th, int n)
     return OPS_OK;
 }
 
+int ops_handle_set_one_pass(ops_handle_t h, int enable)
+{
+    if (!h) return OPS_INVALID_ARGUMENT;
+    h->one_pass = enable != 0;
+    return OPS_OK;
+}
+
 int ops_handle_set_output_malloc(ops_handle_t h, int use_cuda_malloc)
 {
     if (!h) return OPS_INVALID_ARGUMENT;
@@ -694,6 +795,7 @@ int ops_spgemm_symbolic(ops_handle_t h, int32_t rows_a, int32_t cols_a, int32_t 
         cudaStream_t st = static_cast<cudaStream_t>(stream);
         const Mat A{rows_a, cols_a, a_rpt, a_col, nullptr};
         const Mat B{cols_a, cols_b, b_rpt, b_col, nullptr};
+        h->op_dtype = -1;  // no values: two passes
         long long nnz = 0;
         OPS_CHECK(run_symbolic(h, A, B, c_rpt, &nnz, st));
         *c_nnz = nnz;
@@ -752,6 +854,20 @@ int ops_spgemm(ops_handle_t h, int dtype, int32_t rows_a, int32_t cols_a, int32_
         cudaStream_t st = static_cast<cudaStream_t>(stream);
         const Mat A{rows_a, cols_a, a_rpt, a_col, a_val};
         const Mat B{cols_a, cols_b, b_rpt, b_col, b_val};
+        // the values are known before the counting phase: the R16, R32 and W rows may run
+        // their numeric kernels there (one pass); reset whichever way the call returns
+        struct OnePassScope {
+            ops_handle_s *h;
+            ~OnePassScope()
+            {
+                h->op_dtype = -1;
+                h->op_aval = h->op_bval = nullptr;
+                h->staged = false;
+            }
+        } one_pass_scope{h};
+        h->op_dtype = dtype;
+        h->op_aval = a_val;
+        h->op_bval = b_val;
         void *p = nullptr;
         OPS_CUDA(h, out_alloc(h, &p, sizeof(int) * ((size_t)rows_a + 1), st));
         int *rpt = static_cast<int *>(p);

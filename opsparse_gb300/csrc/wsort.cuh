@@ -52,7 +52,7 @@ struct WsortShape {
 // or fold and write (numeric) the runs.  Returns the number of distinct columns.
 template <int PER, int kIdBits, bool kNum, typename T, typename KT>
 __device__ __forceinline__ int wsort_row(const SpgemmArgs<T> &g, int flop, KT *skey, int *heads, const T *sa,
-                                         const T *sb, int off, int n_expect)
+                                         const T *sb, long long off, int n_expect)
 {
     using AccT = Acc<T>;
     using S = typename AccT::S;
@@ -145,10 +145,16 @@ __global__ void __launch_bounds__(WsortShape<PMAX>::kThreads, WsortShape<PMAX>::
         const int a0 = __ldg(g.arpt + r);
         const int a1 = __ldg(g.arpt + r + 1);
         const int flop = __ldg(g.row_flop + r);
-        int off = 0, n_expect = 0;
+        long long off = 0;
+        int n_expect = 0;
         if constexpr (kNum) {
-            off = __ldg(g.c_rpt + r);
-            n_expect = __ldg(g.c_rpt + r + 1) - off;
+            if (g.stage_cap) {  // one-pass: the list entry's staging slot, count unknown
+                off = it * g.stage_cap;
+                n_expect = INT_MAX;
+            } else {
+                off = __ldg(g.c_rpt + r);
+                n_expect = __ldg(g.c_rpt + r + 1) - (int)off;
+            }
         }
         // expansion: windows of 32 A entries, kUnroll chunks of 32 products in flight
         int wbase = 0;
@@ -231,7 +237,7 @@ __global__ void __launch_bounds__(WsortShape<PMAX>::kThreads, WsortShape<PMAX>::
                 }
             }
         }
-        if constexpr (!kNum) {
+        if (!kNum || g.stage_cap) {
             if (lane == 0) {
                 g.c_rpt[r] = total;
                 nnz_acc += (unsigned long long)total;
@@ -241,7 +247,7 @@ __global__ void __launch_bounds__(WsortShape<PMAX>::kThreads, WsortShape<PMAX>::
         }
         __syncwarp();
     }
-    if constexpr (!kNum) warp_add_u64(nnz_acc, &g.info->total_nnz);
+    if (!kNum || g.stage_cap) warp_add_u64(nnz_acc, &g.info->total_nnz);
 }
 
 }  // namespace opsg

@@ -70,6 +70,28 @@ def test_f32(cuda, handle, case):
     assert np.all(val[~nz] == 0)
 
 
+@pytest.mark.parametrize("one_pass", [True, False], ids=["one_pass", "two_pass"])
+@pytest.mark.parametrize("dtype", ["f64", "f32"])
+@pytest.mark.parametrize("case", CASES, ids=IDS)
+def test_oneshot_against_oracle(cuda, case, dtype, one_pass):
+    """ops_spgemm (values known before counting, so rows of at most 128 products may run
+    in one pass through the staging area) is bit-identical to the oracle either way."""
+    name, a, b, ncols = case
+    npd = np.float64 if dtype == "f64" else np.float32
+    a = (a[0], a[1], a[2].astype(npd))
+    b = (b[0], b[1], b[2].astype(npd))
+    with ops.Handle() as h:
+        h.set_one_pass(one_pass)
+        for _ in range(2):  # the second call reuses the staging area
+            rpt, col, val = run_case(cuda, h, (name, a, b, ncols), getattr(cuda, "float64" if dtype == "f64" else
+                                                                           "float32"), oneshot=True)
+            orpt, ocol, oval = oracle.spgemm(*a, *b, ncols, dtype=npd)
+            assert np.array_equal(rpt.astype(np.int64), orpt), name
+            assert np.array_equal(col, ocol), name
+            ut = np.uint64 if dtype == "f64" else np.uint32
+            assert np.array_equal(val.view(ut), oval.view(ut)), name
+
+
 @pytest.mark.parametrize("case", CASES[:4] + CASES[6:7], ids=IDS[:4] + IDS[6:7])
 def test_oneshot_matches_two_phase(cuda, handle, case):
     r1 = run_case(cuda, handle, case, cuda.float64, oneshot=True)
