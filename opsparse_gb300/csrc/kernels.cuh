@@ -565,10 +565,10 @@ constexpr int kWarpRowsThreads = 256;
 constexpr int kCountUnroll = 4;  // symbolic: chunks whose column loads are issued together
 
 // Column-window rows (symbolic): a row whose products all fall within kWinBits consecutive
-// columns (banded and stencil matrices) is counted over a bitmap of that window instead
-// of a hash table: setting a bit needs no probing.  A second-level bitmap (one word per
-// lane) marks the non-zero words, so counting and clearing touch only the words the row
-// set, and the bitmap stays zero between window rows.
+// columns (banded and stencil matrices) is counted over a bitmap of that window instead of
+// a hash table.  Marking a column is one shared-memory OR whose result nobody waits for
+// (no probing, no dependent second access); the row's words are then swept once to count
+// the set bits and clear them, so the bitmap is all-zero between window rows.
 constexpr int kWinBits = 32768;
 constexpr int kWinWords = kWinBits / 32;
 
@@ -576,7 +576,7 @@ template <bool kNum, typename T, int TMAX>
 constexpr size_t warp_rows_per_warp()
 {
     constexpr size_t hash = (size_t)TMAX * (sizeof(int) + (kNum ? sizeof(typename Acc<T>::S) : 0));
-    constexpr size_t win = kNum ? 0 : (size_t)kWinWords * 4 + 32 * 4;
+    constexpr size_t win = kNum ? 0 : (size_t)kWinWords * 4;
     return hash > win ? hash : win;
 }
 
@@ -586,37 +586,60 @@ constexpr size_t warp_rows_smem()
     return (size_t)(kWarpRowsThreads / 32) * warp_rows_per_warp<kNum, T, TMAX>();
 }
 
-// Distinct-column count of one window row, written to c_rpt[r].  bits/l1 are all-zero on
-// entry and on return.  All lanes call it.
+// Column window of a row whose B rows are long: [cmin, cmax] from the first and last
+// column of each B row (B rows are sorted).  cmax < cmin when the row has no products.
 template <typename T>
-__device__ __forceinline__ void window_count_row(const SpgemmArgs<T> &g, int r, int a0, int a1, int cmin, int nbits,
-                                                 unsigned *bits, unsigned *l1, unsigned long long &nnz_acc)
+__device__ __forceinline__ void row_window(const SpgemmArgs<T> &g, int a0, int a1, int &cmin, int &cmax)
 {
     const int lane = lane_id();
+    cmin = INT_MAX;
+    cmax = -1;
+    for (int wa = a0; wa < a1; wa += 32) {
+        const int q = wa + lane;
+        if (q < a1) {
+            const int j = __ldg(g.acol + q);
+            const int b0 = __ldg(g.brpt + j), b1 = __ldg(g.brpt + j + 1);
+            if (b1 > b0) {
+                cmin = min(cmin, __ldg(g.bcol + b0));
+                cmax = max(cmax, __ldg(g.bcol + b1 - 1));
+            }
+        }
+    }
+    cmin = __reduce_min_sync(kFull, cmin);
+    cmax = __reduce_max_sync(kFull, cmax);
+}
+
+// Sets the bits of the row's columns (offsets from cmin, at most span).  Returns true on
+// every lane if a column fell outside [cmin, cmin + span] (a B row out of order).
+template <typename T>
+__device__ __forceinline__ bool window_mark(const SpgemmArgs<T> &g, int a0, int a1, int cmin, int span,
+                                            unsigned *bits)
+{
     bool bad = false;
     warp_rowwise_products_pf<4, false, T>(a0, a1, g.acol, g.aval, g.brpt, g.bcol, g.bval, [&](bool valid, int col, T, T) {
         if (valid) {
             const int o = col - cmin;
-            if ((unsigned)o < (unsigned)nbits) {
-                const int w = o >> 5;
-                if (atomicOr(bits + w, 1u << (o & 31)) == 0u) atomicOr(l1 + (w >> 5), 1u << (w & 31));
-            } else {
-                bad = true;  // only if a B row is not sorted: invalid input
-            }
+            if ((unsigned)o <= (unsigned)span) atomicOr(bits + (o >> 5), 1u << (o & 31));
+            else bad = true;
         }
     });
-    if (__any_sync(kFull, bad) && lane == 0) atomicOr(&g.info->flags, kErrBadColumn);
     __syncwarp();
-    // lane l owns words l*32 .. l*32+31: count the set ones and clear them
+    return __any_sync(kFull, bad);
+}
+
+// Distinct-column count of one window row, written to c_rpt[r].  All lanes call it.
+template <typename T>
+__device__ __forceinline__ void window_count_row(const SpgemmArgs<T> &g, int r, int a0, int a1, int cmin, int cmax,
+                                                 unsigned *bits, unsigned long long &nnz_acc)
+{
+    const int lane = lane_id();
+    if (window_mark<T>(g, a0, a1, cmin, cmax - cmin, bits) && lane == 0) atomicOr(&g.info->flags, kErrBadColumn);
+    const int nw = ((cmax - cmin) >> 5) + 1;
     int cnt = 0;
-    unsigned m = l1[lane];
-    while (m) {
-        const int w = lane * 32 + __ffs(m) - 1;
-        m &= m - 1u;
+    for (int w = lane; w < nw; w += 32) {
         cnt += __popc(bits[w]);
         bits[w] = 0u;
     }
-    l1[lane] = 0u;
     const int total = (int)__reduce_add_sync(kFull, (unsigned)cnt);
     if (lane == 0) {
         g.c_rpt[r] = total;
@@ -634,13 +657,11 @@ __global__ void __launch_bounds__(kWarpRowsThreads) k_warp_rows(SpgemmArgs<T> g,
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int lane = lane_id();
     const int warp = threadIdx.x >> 5;
-    constexpr int kWarps = kWarpRowsThreads / 32;
     const int count = *count_ptr;
     unsigned char *wbase = smem_raw + (size_t)warp * warp_rows_per_warp<kNum, T, TMAX>();
     S *vals = reinterpret_cast<S *>(wbase);
     int *keys = reinterpret_cast<int *>(wbase + (kNum ? sizeof(S) * TMAX : 0));
     unsigned *wbits = reinterpret_cast<unsigned *>(wbase);  // window layout (symbolic)
-    unsigned *wl1 = wbits + kWinWords;
     bool win_clean = false;  // the window bitmap is all-zero (no hash row has used the space since)
     const long long warp0 = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
@@ -665,27 +686,15 @@ __global__ void __launch_bounds__(kWarpRowsThreads) k_warp_rows(SpgemmArgs<T> g,
         const bool rowwise = row_products >= 16 * (a1 - a0);
         if (!kNum && rowwise) {
             // long B rows: do all the products fit a window of kWinBits columns?
-            int cmin = INT_MAX, cmax = -1;
-            for (int wa = a0; wa < a1; wa += 32) {
-                const int q = wa + lane;
-                if (q < a1) {
-                    const int j = __ldg(g.acol + q);
-                    const int b0 = __ldg(g.brpt + j), b1 = __ldg(g.brpt + j + 1);
-                    if (b1 > b0) {
-                        cmin = min(cmin, __ldg(g.bcol + b0));
-                        cmax = max(cmax, __ldg(g.bcol + b1 - 1));
-                    }
-                }
-            }
-            cmin = __reduce_min_sync(kFull, cmin);
-            cmax = __reduce_max_sync(kFull, cmax);
+            int cmin, cmax;
+            row_window<T>(g, a0, a1, cmin, cmax);
             if (cmax >= cmin && cmax - cmin < kWinBits) {
                 if (!win_clean) {
-                    for (int i = lane; i < kWinWords + 32; i += 32) wbits[i] = 0u;
+                    for (int i = lane; i < kWinWords; i += 32) wbits[i] = 0u;
                     __syncwarp();
                     win_clean = true;
                 }
-                window_count_row<T>(g, r, a0, a1, cmin, kWinBits, wbits, wl1, nnz_acc);
+                window_count_row<T>(g, r, a0, a1, cmin, cmax, wbits, nnz_acc);
                 continue;
             }
         }
