@@ -195,6 +195,42 @@ def run_reference(args, desc, dt, data, n, rank, world):
 
 
 # ----------------------------------------------------------------------------- GPU side
+def cusparse_gpu(A, B, n, P, nnz_c, t_ms, flush, iters=10):
+    """cuSPARSE's SpGEMM on the same device-resident inputs (torch's CSR x CSR product,
+    which calls cusparseSpGEMM), timed like this library's steps: L2 flushed before each
+    call, CUDA events around the call, 1 warm-up then the mean of `iters` calls.  A
+    side-by-side comparison only; nothing here is on the library's path."""
+    import torch
+
+    try:
+        def csr(m):
+            return torch.sparse_csr_tensor(m.rpt.long(), m.col.long(), m.val, size=(m.rows, m.cols))
+
+        a, b = csr(A), csr(B)
+        ts = []
+        nnz_cs = -1
+        for i in range(iters + 1):
+            flush.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            e0.record()
+            c = torch.sparse.mm(a, b)
+            e1.record()
+            torch.cuda.synchronize()
+            if i:
+                ts.append(e0.elapsed_time(e1))
+            nnz_cs = int(c._nnz())
+            del c
+        del a, b
+    except Exception as e:  # a comparison, never the product
+        return {"unavailable": f"{type(e).__name__}: {e}".splitlines()[0][:200]}
+    ms = float(np.mean(ts))
+    return {"impl": "cuSPARSE SpGEMM through torch.sparse.mm on CSR tensors (int64 indices, as torch requires)",
+            "protocol": "1 warm-up + mean of 10 calls, CUDA events, L2 flushed before each call",
+            "ms_per_call": ms, "GFLOPS": 2.0 * P / (ms * 1e-3) / 1e9, "nnz_c": nnz_cs,
+            "nnz_c_equal": nnz_cs == nnz_c, "speedup_of_this_library": ms / t_ms}
+
+
 def reference_gpu(A, B, n, P, nnz_c, t_ms, flush, iters=10):
     """OpSparse's own kernels on this GPU (oracle/ref_gpu), timed with its own benchmark
     protocol: 1 warm-up, then the mean of 10 calls, each wall-clocked around the whole call
@@ -246,7 +282,7 @@ def run_ours(args, desc, dt, data, n, rank, world, local_rank):
     B = A if same else ops.csr_to_device(brpt, bcol, bval, n, n, dtype=tdt, device=str(dev))
     lib = capi.load()
     h = ops.Handle()
-    h.set_one_pass(args.one_pass)
+    h.set_one_pass(1 if args.one_pass else 0)
     stream = torch.cuda.current_stream()
     st = C.c_void_p(stream.cuda_stream)
     code = capi.OPS_F64 if dt == "f64" else capi.OPS_F32
@@ -373,6 +409,8 @@ def run_ours(args, desc, dt, data, n, rank, world, local_rank):
     }
     if dt == "f64" and world == 1 and args.reference_gpu:
         line["reference_gpu"] = reference_gpu(A, B, n, P, nnz_c, t_ms, flush)
+    if world == 1 and args.cusparse:
+        line["cusparse_gpu"] = cusparse_gpu(A, B, n, P, nnz_c, t_ms, flush)
     if args.cpu_baseline and world == 1:
         t_cpu, cores = cpu_baseline(data, n)
         line["cpu_baseline"] = {"value": 2.0 * P / t_cpu / 1e9, "unit": "GFLOPS", "cores": cores, "kind": "port",
@@ -393,6 +431,8 @@ def main():
                              "backward_f32"])
     ap.add_argument("--batch", type=int, default=4096, help="problems in the batched workload")
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
+    ap.add_argument("--no-cusparse", dest="cusparse", action="store_false",
+                    help="skip timing cuSPARSE's SpGEMM on the same inputs")
     ap.add_argument("--two-pass", dest="one_pass", action="store_false",
                     help="count and compute every row in separate passes (no staging of short rows)")
     ap.add_argument("--no-reference-gpu", dest="reference_gpu", action="store_false",

@@ -85,15 +85,19 @@ int ops_handle_set_dense_budget(ops_handle_t handle, size_t bytes);
  * with ops_free; 1 = cudaMalloc, release with cudaFree (what OpSparse's CSR::drelease
  * expects). */
 int ops_handle_set_output_malloc(ops_handle_t handle, int use_cuda_malloc);
-/* One-pass rows in ops_spgemm (default 1 = on): rows of at most 128 intermediate products
- * (the R16, R32 and W classes) compute their values during the counting phase into a
- * staging area held by the handle (grow-only, at most 2 GiB; beyond that, or if it cannot
- * be allocated, the call falls back to two passes) and are copied into C after the row_ptr
- * scan, instead of re-reading A and B in a second pass.  Results are identical either way.
- * ops_spgemm_symbolic / ops_spgemm_numeric always run two passes.  No OpSparse
- * counterpart: its symbolic and numeric kernels always run separately
- * (core_algo/spgemm/spgemm.cu:16-62). */
-int ops_handle_set_one_pass(ops_handle_t handle, int enable);
+/* One pass in ops_spgemm, where the values are known before the counting phase.  mode 1
+ * (default): when at least 2^20 products are eligible, every row except those above 13312
+ * products, the rows of 129 to 1024 products that have more than 512 products or whose
+ * products fall within 32768 consecutive columns (banded and stencil rows, which fold many
+ * products per output) is computed during the counting phase into
+ * a staging area held by the handle, then copied into C after the row_ptr scan, instead
+ * of reading A and B again in a second pass.  The area grows only and holds the eligible
+ * products (column and value each), at most 2 GiB; beyond that, or if it cannot be
+ * allocated, the call runs two passes.  mode 2: the same at any size.  mode 0: always two
+ * passes.  Results are identical in every mode.  ops_spgemm_symbolic and
+ * ops_spgemm_numeric always run two passes.  No OpSparse counterpart: its symbolic and
+ * numeric kernels always run separately (core_algo/spgemm/spgemm.cu:16-62). */
+int ops_handle_set_one_pass(ops_handle_t handle, int mode);
 /* Row-class thresholds used by the next symbolic phase, as 6 int32 upper bounds on a
  * row's intermediate products: {R8, R16, R32, W, E1, E2} (defaults {8, 16, 32, 128, 1024,
  * 13312}, which are also the maxima; 0 switches a class off; rows above E2 use the dense

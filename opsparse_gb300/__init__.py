@@ -116,9 +116,9 @@ class Handle:
         check(self.lib.ops_handle_get_thresholds(self.h, arr, 6), self.h)
         return list(arr)
 
-    def set_one_pass(self, enable: bool):
-        """Rows of at most 128 products computed during the counting phase (ops_spgemm only)."""
-        check(self.lib.ops_handle_set_one_pass(self.h, int(bool(enable))), self.h)
+    def set_one_pass(self, mode: int):
+        """ops_spgemm in one pass: 0 off, 1 on for large inputs (default), 2 on at any size."""
+        check(self.lib.ops_handle_set_one_pass(self.h, int(mode)), self.h)
 
     def set_dense_budget(self, nbytes: int):
         check(self.lib.ops_handle_set_dense_budget(self.h, int(nbytes)), self.h)

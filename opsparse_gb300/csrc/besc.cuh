@@ -170,7 +170,7 @@ __device__ __forceinline__ int besc_sort_fold(const SpgemmArgs<T> &g, int n, int
         }
         if (tid == 0) hidx[total] = n;
         __syncthreads();
-        if (tid == 0 && total != n_expect) atomicOr(&g.info->flags, kErrCountMismatch);
+        if (tid == 0 && !g.soff && total != n_expect) atomicOr(&g.info->flags, kErrCountMismatch);
         // runs in head order: consecutive threads write consecutive entries of C.  A run
         // is folded kUnroll products at a time, their operands loaded together.
         for (int hh = tid; hh < total; hh += NT) {
@@ -252,8 +252,13 @@ __global__ void __launch_bounds__(Shape::kThreads, Shape::kMinBlocks) k_besc_row
         const int n = esc_scan_row<NT, T>(g, a0, lenA, s_incl, s_b0, s_warp_sums);
         int off = 0, n_expect = 0;
         if constexpr (kNum) {
-            off = __ldg(g.c_rpt + r);
-            n_expect = __ldg(g.c_rpt + r + 1) - off;
+            if (g.soff) {  // one-pass: the row's staging slot, count unknown
+                off = __ldg(g.soff + r);
+                n_expect = INT_MAX;
+            } else {
+                off = __ldg(g.c_rpt + r);
+                n_expect = __ldg(g.c_rpt + r + 1) - off;
+            }
         }
         // expansion: kUnroll chunks of 32 products per warp, loads in flight together
         bool bad = false;
@@ -295,7 +300,7 @@ __global__ void __launch_bounds__(Shape::kThreads, Shape::kMinBlocks) k_besc_row
             total = besc_sort_fold<Shape, P, kIdBits, kNum, T, KT>(g, m, a0, skeys, spid, hidx, own, s_incl, s_b0,
                                                                    off, n_expect, s_warp_sums, s_last);
         }
-        if constexpr (!kNum) {
+        if (!kNum || g.soff) {
             if (tid == 0) {
                 g.c_rpt[r] = total;
                 nnz_acc += (unsigned long long)total;
@@ -303,9 +308,7 @@ __global__ void __launch_bounds__(Shape::kThreads, Shape::kMinBlocks) k_besc_row
         }
         __syncthreads();
     }
-    if constexpr (!kNum) {
-        if (tid == 0 && nnz_acc) atomicAdd(&g.info->total_nnz, nnz_acc);
-    }
+    if (tid == 0 && nnz_acc) atomicAdd(&g.info->total_nnz, nnz_acc);
 }
 
 }  // namespace opsg

@@ -28,7 +28,18 @@ enum RowClass : int {
 
 // Extra device lists after the kNumClasses class lists: the numeric re-binning of the E1
 // rows and the size split of the E2 rows.
-enum : int { kXlE1Sort = 0, kXlE1Hash = 1, kXlE1Esc = 2, kXlE2Mid = 3, kXlE2Large = 4, kNumExtraLists = 5 };
+// The last two split the E1 rows of a one-pass call into those computed in the counting
+// phase and those left to two passes.
+enum : int {
+    kXlE1Sort = 0,
+    kXlE1Hash = 1,
+    kXlE1Esc = 2,
+    kXlE2Mid = 3,
+    kXlE2Large = 4,
+    kXlE1One = 5,
+    kXlE1Two = 6,
+    kNumExtraLists = 7
+};
 constexpr int kNumLists = kNumClasses + kNumExtraLists;
 
 constexpr int kSmallFlopMax = 8;   // R8 rows: symbolic inside k_setup, numeric k_small_rows
@@ -37,6 +48,14 @@ constexpr int kEsc1FlopMax = 1024;
 constexpr int kEsc1AMax = 1024;
 constexpr int kEsc2FlopMax = 13312;
 constexpr int kEsc2AMax = 2560;
+// E1 rows computed in the counting phase of a one-pass call (warp sort of at most this
+// many products); heavier E1 rows keep two passes, and so do column-window rows (below)
+constexpr int kE1OnePassFlopMax = 512;
+// Column-window rows: rows whose B rows are long (at least 16 products per A entry) and
+// whose products all fall within kWinBits consecutive columns (banded and stencil
+// matrices).  They fold many products per output: counted over a window bitmap, computed
+// through a hash table, never sorted product by product.
+constexpr int kWinBits = 32768;
 
 // Runtime row-class thresholds (the autotuner's search space).  Each bound is capped by
 // the compiled capacity of its kernel; a bound of 0 switches the class off.
@@ -70,6 +89,9 @@ struct DevInfo {
     int split[3];                 // E1 rows re-binned for the numeric phase: [warp sort, hash, expand/sort]
     int split2[2];                // E2 rows by size, fixed at the symbolic phase: [mid shape, large shape]
     int next_mid[2];              // row cursor of the mid-shape E2 kernel [symbolic, numeric]
+    int split1[2];                // E1 rows of a one-pass call: [one pass (flop <= kWsortFlopMax), two passes]
+    unsigned long long staged_flop;  // products of the rows a one-pass call may stage
+    int e1_one;                   // E1 rows a one-pass call may stage
     unsigned long long d_len_a;   // A entries of the D rows
     unsigned long long d_flop;    // products of the D rows
     int d_cursor;                 // output cursor of the D-row expansion
@@ -92,11 +114,12 @@ struct SpgemmArgs {
     int *c_col;
     T *c_val;
     DevInfo *info;
-    // One-pass numeric (register and W rows, run inside the counting phase): when > 0,
-    // the row at list index i writes its entries to c_col/c_val + i * stage_cap (a
-    // staging area), its count to c_rpt[r] and the count to info->total_nnz, as the
-    // counting kernels do; k_place_staged moves the entries to C after the scan.
-    int stage_cap;
+    // One-pass numeric (run inside the counting phase, values known): when set, row r
+    // writes its entries to c_col/c_val + soff[r] (a staging area holding every staged
+    // row's products at the exclusive prefix of their counts), its count to c_rpt[r] and
+    // the count to info->total_nnz, as the counting kernels do; k_place_staged moves the
+    // entries into C after the scan.
+    const int *soff;
 };
 
 __device__ __forceinline__ int lane_id() { return threadIdx.x & 31; }

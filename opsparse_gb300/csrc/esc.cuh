@@ -251,8 +251,9 @@ __global__ void __launch_bounds__(Shape::kThreads, 1) k_esc_rows(SpgemmArgs<T> g
             __syncthreads();
         } else {
             // ----------------------------------------------------------- numeric --
-            const int off = __ldg(g.c_rpt + r);
-            const int n_expect = __ldg(g.c_rpt + r + 1) - off;
+            // one-pass: the row's staging slot, count unknown until the runs are found
+            const int off = g.soff ? __ldg(g.soff + r) : __ldg(g.c_rpt + r);
+            const int n_expect = g.soff ? INT_MAX : __ldg(g.c_rpt + r + 1) - off;
             const int n = flop;
             for (int c0 = warp * 32; c0 < n; c0 += kUnroll * NT) {
                 int oo[kUnroll], kk[kUnroll];
@@ -367,7 +368,11 @@ __global__ void __launch_bounds__(Shape::kThreads, 1) k_esc_rows(SpgemmArgs<T> g
             if (tid == 0) s_count = 0;
             int total = 0;
             const int hincl = block_inclusive_scan(heads, s_warp_sums, &total);
-            if (tid == 0 && total != n_expect) atomicOr(&g.info->flags, kErrCountMismatch);
+            if (tid == 0 && !g.soff && total != n_expect) atomicOr(&g.info->flags, kErrCountMismatch);
+            if (tid == 0 && g.soff) {
+                g.c_rpt[r] = total;
+                nnz_acc += (unsigned long long)total;
+            }
             int *hidx = reinterpret_cast<int *>(kout);
             const int hs = hincl - heads, he = hincl;
             for (int i = ib, h = hs; i < ie; ++i)
@@ -426,7 +431,7 @@ __global__ void __launch_bounds__(Shape::kThreads, 1) k_esc_rows(SpgemmArgs<T> g
             __syncthreads();
         }
     }
-    if constexpr (!kNum) block_add_u64(nnz_acc, &g.info->total_nnz);
+    if (!kNum || g.soff) block_add_u64(nnz_acc, &g.info->total_nnz);
 }
 
 // Device-side re-binning of a class list into kWays sub-lists (out + w*stride), with
@@ -474,6 +479,12 @@ struct PickE1 {
         if (f <= sort_flop_max && f < 2 * nnz) return 0;
         return nnz <= kSplitNnz ? 1 : 2;
     }
+};
+
+// Rows of a one-pass call: 0 = staged (a staging slot of one or more products), 1 = not.
+struct PickStaged {
+    const int *soff;
+    __device__ int operator()(int r) const { return soff[r + 1] > soff[r] ? 0 : 1; }
 };
 
 // E2 rows by size: 0 = mid shape (EscMid), 1 = large shape (EscLarge).

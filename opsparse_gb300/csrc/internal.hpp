@@ -67,17 +67,21 @@ struct ops_handle_s {
     size_t dense_bytes = 0;
     int dense_ctas = 0;
 
-    // one-pass numeric of the R16, R32 and W rows (ops_spgemm, where the values are known
-    // before the counting phase): their numeric kernels run in the counting phase into a
-    // staging area (grow-only) and are placed into C after the scan
-    bool one_pass = true;          // allowed on this handle
+    // one-pass numeric (ops_spgemm, where the values are known before the counting
+    // phase): every row but the D rows, the E1 rows above kE1OnePassFlopMax products and
+    // the E1 column-window rows is computed in the counting phase into a staging area
+    // (grow-only) at the exclusive prefix of the staged rows' product counts, and moved
+    // into C after the scan
+    int one_pass = 1;              // 0 off, 1 on above kMinStageFlop staged products, 2 on
     int op_dtype = -1;             // value type of the call in progress, -1 = two passes
     const void *op_aval = nullptr, *op_bval = nullptr;
-    bool staged = false;           // the counting phase just staged those classes
-    unsigned char *stage = nullptr;
+    bool staged = false;           // the counting phase of the call in progress stages
+    bool stage_e1 = false;         // ... and some of its rows are E1 rows
+    unsigned char *stage = nullptr;        // [columns | values] of stage_entries entries
     size_t stage_bytes = 0;
+    long long stage_entries = 0;
     size_t stage_budget = size_t(2) << 30;  // larger staging areas fall back to two passes
-    size_t stage_off[kNumClasses] = {};  // byte offsets of a class's [columns | values]
+    int *soff = nullptr;           // [M + 1] staged products per row, then their prefix (workspace)
 
     // plan of the last symbolic phase
     bool plan_valid = false;

@@ -126,18 +126,23 @@ static __global__ void __launch_bounds__(kSetupThreads) k_setup(const int *__res
                                                         const int *__restrict__ brpt, const int *__restrict__ bcol,
                                                         int M, int K, int N, int *__restrict__ row_flop,
                                                         int *__restrict__ lists, int *__restrict__ c_rownnz,
-                                                        DevInfo *info, Thresholds th)
+                                                        int *__restrict__ sflop, DevInfo *info, Thresholds th)
 {
     static_assert(kSmallFlopMax == kSetupUnroll, "R8 rows are gathered from the light-row registers");
     __shared__ int s_cnt[kNumClasses];
     __shared__ int s_base[kNumClasses];
     __shared__ unsigned long long s_flop[kSetupThreads / 32];
+    __shared__ unsigned long long s_sflop[kSetupThreads / 32];
+    __shared__ int s_e1one;
     __shared__ unsigned s_small[kSetupThreads / 32];
     __shared__ int s_flags;
     const int lane = lane_id();
     const int warp = threadIdx.x >> 5;
     if (threadIdx.x < kNumClasses) s_cnt[threadIdx.x] = 0;
-    if (threadIdx.x == 0) s_flags = 0;
+    if (threadIdx.x == 0) {
+        s_flags = 0;
+        s_e1one = 0;
+    }
     __syncthreads();
 
     const int r = blockIdx.x * kSetupThreads + threadIdx.x;
@@ -273,11 +278,46 @@ static __global__ void __launch_bounds__(kSetupThreads) k_setup(const int *__res
             if (cls == c) my_off = base + __popc(mk & lanemask_lt());
         }
     }
+    // products a one-pass call may compute in the counting phase (every class but D and
+    // the heavier E1 rows), for the prefix that places them in the staging area
+    int staged = 0;
+    if (sflop) {
+        staged = (cls >= 0 && cls != kClsD && (cls != kClsE1 || f32 <= kE1OnePassFlopMax)) ? f32 : 0;
+        if (cls == kClsE1 && staged && f32 >= 16 * lenA) {
+            // a column-window row keeps two passes: span of its B rows' first and last
+            // columns (B rows are sorted; lenA <= 32 here)
+            int cmin = INT_MAX, cmax = -1;
+            if (light) {
+#pragma unroll
+                for (int u = 0; u < kSetupUnroll; ++u) {
+                    if (u < lenA && bl[u] > 0) {
+                        cmin = min(cmin, __ldg(bcol + b0[u]));
+                        cmax = max(cmax, __ldg(bcol + b0[u] + bl[u] - 1));
+                    }
+                }
+            } else {
+                for (int p = a0; p < a1; ++p) {
+                    const int j = __ldg(acol + p);
+                    if ((unsigned)j >= (unsigned)K) continue;  // reported above
+                    const int q0 = __ldg(brpt + j), q1 = __ldg(brpt + j + 1);
+                    if (q1 > q0) {
+                        cmin = min(cmin, __ldg(bcol + q0));
+                        cmax = max(cmax, __ldg(bcol + q1 - 1));
+                    }
+                }
+            }
+            if (cmax >= cmin && cmax - cmin < kWinBits) staged = 0;
+        }
+        if (in) sflop[r] = staged;
+        if (cls == kClsE1 && staged) atomicAdd(&s_e1one, 1);
+    }
+    const unsigned long long wsf = warp_sum_u64((unsigned long long)staged);
     unsigned long long wf = warp_sum_u64((unsigned long long)flop);
     const unsigned wmax = __reduce_max_sync(kFull, (unsigned)f32);
     const unsigned wsmall = __reduce_add_sync(kFull, small_nnz);
     if (lane == 0) {
         s_flop[warp] = wf;
+        s_sflop[warp] = wsf;
         s_small[warp] = wsmall;
     }
     __syncthreads();
@@ -289,6 +329,10 @@ static __global__ void __launch_bounds__(kSetupThreads) k_setup(const int *__res
         unsigned long long t = 0;
         for (int w = 0; w < kSetupThreads / 32; ++w) t += s_flop[w];
         if (t) atomicAdd(&info->total_flop, t);
+        unsigned long long ts = 0;
+        for (int w = 0; w < kSetupThreads / 32; ++w) ts += s_sflop[w];
+        if (ts) atomicAdd(&info->staged_flop, ts);
+        if (s_e1one) atomicAdd(&info->e1_one, s_e1one);
         unsigned long long sn = 0;
         for (int w = 0; w < kSetupThreads / 32; ++w) sn += s_small[w];
         if (sn) atomicAdd(&info->total_nnz, sn);
@@ -384,8 +428,9 @@ __global__ void __launch_bounds__(kSmallThreads, 4) k_small_rows(SpgemmArgs<T> g
         OPSG_CS(1, 4); OPSG_CS(3, 6);
         OPSG_CS(1, 2); OPSG_CS(3, 4); OPSG_CS(5, 6);
 #undef OPSG_CS
-        const int off = __ldg(g.c_rpt + r);
-        const int n_expect = __ldg(g.c_rpt + r + 1) - off;
+        // one-pass: the staging slot of the row; c_rpt[r] still holds the row's count
+        const int off = g.soff ? __ldg(g.soff + r) : __ldg(g.c_rpt + r);
+        const int n_expect = g.soff ? __ldg(g.c_rpt + r) : __ldg(g.c_rpt + r + 1) - off;
         typename AccT::S acc = AccT::zero();
         int pos = 0;
 #pragma unroll
@@ -484,9 +529,9 @@ __global__ void __launch_bounds__(256) k_reg_rows(SpgemmArgs<T> g, const int *__
                 const int lt = __shfl_sync(kFull, (int)leader, t, G);
                 rank += (lt && ct < col) ? 1 : 0;
             }
-            if (g.stage_cap) {  // one-pass: staging slot of the list entry, count as symbolic
+            if (g.soff) {  // one-pass: staging slot of the row, count as symbolic
                 if (leader) {
-                    const long long pos = gid * g.stage_cap + rank;
+                    const int pos = __ldg(g.soff + r) + rank;
                     g.c_col[pos] = col;
                     g.c_val[pos] = AccT::fin(s);
                 }
@@ -502,27 +547,115 @@ __global__ void __launch_bounds__(256) k_reg_rows(SpgemmArgs<T> g, const int *__
             }
         }
     }
-    if (!kNum || g.stage_cap) warp_add_u64(nnz_acc, &g.info->total_nnz);
+    if (!kNum || g.soff) warp_add_u64(nnz_acc, &g.info->total_nnz);
 }
 
-// Moves staged rows (one-pass numeric) into C: list entry i's slot at i << log_cap holds
-// the row's c_rpt[r+1] - c_rpt[r] entries.  One thread per slot, so the staging area is
-// read and C written in order.
+// Moves the staged rows of a one-pass call into C, in row order: row r was staged if
+// soff[r + 1] > soff[r] (its staging slot holds up to its product count), and its
+// c_rpt[r + 1] - c_rpt[r] entries go to C from c_rpt[r] on.  A warp takes 32 consecutive
+// rows and walks the concatenation of their entries 32 at a time, each lane finding the
+// row of its entry by a binary search over the warp's prefix of counts, with kPlaceUnroll
+// chunks' loads in flight together: C is written contiguously and the staging area read
+// almost so (its slots follow row order).
+constexpr int kPlaceUnroll = 4;
+
+// Rows of more than long_flop products are skipped here and copied by k_place_long, so
+// that no warp is left with a long serial copy.
 template <typename T>
-__global__ void k_place_staged(const int *__restrict__ list, int count, int log_cap, const int *__restrict__ scol,
-                               const T *__restrict__ sval, const int *__restrict__ c_rpt, int *__restrict__ c_col,
-                               T *__restrict__ c_val)
+__global__ void __launch_bounds__(256) k_place_staged(int M, const int *__restrict__ soff,
+                                                      const int *__restrict__ c_rpt, const int *__restrict__ row_flop,
+                                                      int long_flop, const int *__restrict__ scol,
+                                                      const T *__restrict__ sval, int *__restrict__ c_col,
+                                                      T *__restrict__ c_val)
 {
-    const long long total = (long long)count << log_cap;
-    const int mask = (1 << log_cap) - 1;
-    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < total;
-         t += (long long)gridDim.x * blockDim.x) {
-        const int r = __ldg(list + (t >> log_cap));
-        const int e = (int)t & mask;
+    const int lane = lane_id();
+    const long long warp0 = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
+    for (long long w = warp0; w * 32 < M; w += nwarps) {
+        const int r = (int)(w * 32) + lane;
+        int so = 0, o = 0, n = 0;
+        if (r < M) {
+            so = __ldg(soff + r);
+            if (__ldg(soff + r + 1) > so && __ldg(row_flop + r) <= long_flop) {
+                o = __ldg(c_rpt + r);
+                n = __ldg(c_rpt + r + 1) - o;
+            }
+        }
+        int incl = n;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const int t = __shfl_up_sync(kFull, incl, d);
+            if (lane >= d) incl += t;
+        }
+        const int total = __shfl_sync(kFull, incl, 31);
+        for (int base = 0; base < total; base += 32 * kPlaceUnroll) {
+            int src[kPlaceUnroll], dst[kPlaceUnroll];
+#pragma unroll
+            for (int u = 0; u < kPlaceUnroll; ++u) {
+                const int e = base + u * 32 + lane;
+                int lo = 0;  // lanes whose rows end at or before entry e
+#pragma unroll
+                for (int step = 16; step >= 1; step >>= 1) {
+                    const int v = __shfl_sync(kFull, incl, lo + step - 1);
+                    if (v <= e) lo += step;
+                }
+                const int l = min(lo, 31);
+                const int first = __shfl_sync(kFull, incl, l) - __shfl_sync(kFull, n, l);
+                const int s0 = __shfl_sync(kFull, so, l);
+                const int o0 = __shfl_sync(kFull, o, l);
+                src[u] = e < total ? s0 + (e - first) : -1;
+                dst[u] = o0 + (e - first);
+            }
+            int cv[kPlaceUnroll];
+            T vv[kPlaceUnroll];
+#pragma unroll
+            for (int u = 0; u < kPlaceUnroll; ++u) {
+                cv[u] = src[u] >= 0 ? __ldg(scol + src[u]) : 0;
+                vv[u] = src[u] >= 0 ? __ldg(sval + src[u]) : T(0);
+            }
+#pragma unroll
+            for (int u = 0; u < kPlaceUnroll; ++u) {
+                if (src[u] >= 0) {
+                    c_col[dst[u]] = cv[u];
+                    c_val[dst[u]] = vv[u];
+                }
+            }
+        }
+    }
+}
+
+// The long staged rows (a class list): one CTA per row, kPlaceUnroll entries per thread
+// in flight.
+template <typename T>
+__global__ void __launch_bounds__(256) k_place_long(const int *__restrict__ list, const int *count_ptr,
+                                                    const int *__restrict__ soff, const int *__restrict__ c_rpt,
+                                                    const int *__restrict__ scol, const T *__restrict__ sval,
+                                                    int *__restrict__ c_col, T *__restrict__ c_val)
+{
+    const int count = *count_ptr;
+    for (int i = blockIdx.x; i < count; i += gridDim.x) {
+        const int r = __ldg(list + i);
+        const int so = __ldg(soff + r);
+        if (__ldg(soff + r + 1) <= so) continue;  // not staged (block-uniform)
         const int o = __ldg(c_rpt + r);
-        if (e < __ldg(c_rpt + r + 1) - o) {
-            c_col[o + e] = scol[t];
-            c_val[o + e] = sval[t];
+        const int n = __ldg(c_rpt + r + 1) - o;
+        for (int base = 0; base < n; base += kPlaceUnroll * (int)blockDim.x) {
+            int cv[kPlaceUnroll];
+            T vv[kPlaceUnroll];
+#pragma unroll
+            for (int u = 0; u < kPlaceUnroll; ++u) {
+                const int e = base + u * (int)blockDim.x + (int)threadIdx.x;
+                cv[u] = e < n ? __ldg(scol + so + e) : 0;
+                vv[u] = e < n ? __ldg(sval + so + e) : T(0);
+            }
+#pragma unroll
+            for (int u = 0; u < kPlaceUnroll; ++u) {
+                const int e = base + u * (int)blockDim.x + (int)threadIdx.x;
+                if (e < n) {
+                    c_col[o + e] = cv[u];
+                    c_val[o + e] = vv[u];
+                }
+            }
         }
     }
 }
@@ -569,7 +702,6 @@ constexpr int kCountUnroll = 4;  // symbolic: chunks whose column loads are issu
 // a hash table.  Marking a column is one shared-memory OR whose result nobody waits for
 // (no probing, no dependent second access); the row's words are then swept once to count
 // the set bits and clear them, so the bitmap is all-zero between window rows.
-constexpr int kWinBits = 32768;
 constexpr int kWinWords = kWinBits / 32;
 
 template <bool kNum, typename T, int TMAX>

@@ -105,8 +105,9 @@ int ensure_ws(ops_handle_s *h, int M, cudaStream_t st)
     // E2 rows by size
     const size_t lists_b = align_up(sizeof(int) * (size_t)(kNumLists) * (size_t)M, 256);
     const size_t flop_b = align_up(sizeof(int) * (size_t)M, 256);
+    const size_t soff_b = align_up(sizeof(int) * ((size_t)M + 1), 256);
     const size_t info_b = align_up(sizeof(DevInfo), 256);
-    const size_t total = lists_b + flop_b + info_b + align_up(cub_bytes, 256);
+    const size_t total = lists_b + flop_b + soff_b + info_b + align_up(cub_bytes, 256);
     if (h->ws) {
         OPS_CUDA(h, cudaFreeAsync(h->ws, st));
         h->ws = nullptr;
@@ -118,8 +119,9 @@ int ensure_ws(ops_handle_s *h, int M, cudaStream_t st)
     h->ws_M = M;
     h->lists = reinterpret_cast<int *>(h->ws);
     h->row_flop = reinterpret_cast<int *>(h->ws + lists_b);
-    h->info = reinterpret_cast<DevInfo *>(h->ws + lists_b + flop_b);
-    h->cub_tmp = h->ws + lists_b + flop_b + info_b;
+    h->soff = reinterpret_cast<int *>(h->ws + lists_b + flop_b);
+    h->info = reinterpret_cast<DevInfo *>(h->ws + lists_b + flop_b + soff_b);
+    h->cub_tmp = h->ws + lists_b + flop_b + soff_b + info_b;
     h->cub_bytes = cub_bytes;
     h->plan_valid = false;
     return OPS_OK;
@@ -166,19 +168,28 @@ int grid_for(long long work_items, int per_block, int cap)
     return (int)std::max<long long>(1, std::min<long long>(b, cap));
 }
 
-// Staging capacity (entries per row) of the classes with a one-pass numeric.
-constexpr int stage_cap_of(int c) { return c == kClsR16 ? 16 : c == kClsR32 ? 32 : c == kClsW ? kWarpFlopMax : 0; }
+// Classes whose rows a one-pass call computes in the counting phase: all but D, and E1
+// only if some E1 row is staged (at most kE1OnePassFlopMax products, not a column-window
+// row; the split is made on the device, without such rows the E1 class keeps its own
+// list and two passes).
+bool staged_class(const ops_handle_s *h, int c) { return c != kClsD && (c != kClsE1 || h->stage_e1); }
 
+// Below this many staged products the set-up of a one-pass call (the offset scan, the
+// copy into C) costs more than the counting kernels it saves.
+constexpr unsigned long long kMinStageFlop = 1ull << 20;
+
+// Values region of the staging area (after the columns of staged_flop entries).
 template <typename T>
-T *stage_vals(ops_handle_s *h, int c, int n)
+T *stage_vals(ops_handle_s *h)
 {
-    return reinterpret_cast<T *>(h->stage + h->stage_off[c] + align_up(sizeof(int) * (size_t)n * stage_cap_of(c), 256));
+    return reinterpret_cast<T *>(h->stage + align_up(sizeof(int) * (size_t)h->stage_entries, 256));
 }
 
-// Counting phase of a one-pass call: class c's numeric kernel writes the rows' entries
-// to the staging area and their counts to c_rpt, in place of the counting kernel.
+// Counting phase of a one-pass call: class c's numeric kernels write its rows' entries
+// to the staging area at soff[r] and their counts to c_rpt, in place of the counting
+// kernels.  The E1 rows it does not stage are counted as usual.
 template <typename T, typename GA>
-void launch_staged_numeric(ops_handle_s *h, const GA &gs, int c, const int *list, int n, cudaStream_t s)
+int launch_staged_class(ops_handle_s *h, const GA &gs, int c, const int *list, int n, cudaStream_t s)
 {
     SpgemmArgs<T> g{};
     g.arpt = gs.arpt;
@@ -193,45 +204,126 @@ void launch_staged_numeric(ops_handle_s *h, const GA &gs, int c, const int *list
     g.row_flop = gs.row_flop;
     g.c_rpt = gs.c_rpt;
     g.info = gs.info;
-    g.stage_cap = stage_cap_of(c);
-    g.c_col = reinterpret_cast<int *>(h->stage + h->stage_off[c]);
-    g.c_val = stage_vals<T>(h, c, n);
+    g.soff = h->soff;
+    g.c_col = reinterpret_cast<int *>(h->stage);
+    g.c_val = stage_vals<T>(h);
     const int sms = h->num_sms;
-    if (c == kClsR16) {
-        k_reg_rows<16, true, T><<<grid_for((n + 1) / 2, 8, sms * 8), 256, 0, s>>>(g, list, n);
-    } else if (c == kClsR32) {
-        k_reg_rows<32, true, T><<<grid_for(n, 8, sms * 8), 256, 0, s>>>(g, list, n);
-    } else {
-        using Sh = WsortShape<4>;
-        const int grid = grid_for(n, Sh::kWarps, sms * 8);
-        if (g.N <= (1 << (32 - Sh::kIdBits))) {
-            k_wsort_rows<4, true, T, unsigned>
-                <<<grid, Sh::kThreads, Sh::smem<true, T, unsigned>(), s>>>(g, list, &h->info->counts[c]);
-        } else {
-            k_wsort_rows<4, true, T, unsigned long long>
-                <<<grid, Sh::kThreads, Sh::smem<true, T, unsigned long long>(), s>>>(g, list, &h->info->counts[c]);
+    const size_t M = (size_t)h->plan_M;
+    int *xl = h->lists + (size_t)kNumClasses * M;
+    switch (c) {
+        case kClsR8:
+            k_small_rows<T><<<grid_for(g.M, kSmallThreads, sms * 8), kSmallThreads, 0, s>>>(g, h->plan_th.r8);
+            break;
+        case kClsR16:
+            k_reg_rows<16, true, T><<<grid_for((n + 1) / 2, 8, sms * 8), 256, 0, s>>>(g, list, n);
+            break;
+        case kClsR32:
+            k_reg_rows<32, true, T><<<grid_for(n, 8, sms * 8), 256, 0, s>>>(g, list, n);
+            break;
+        case kClsW: {
+            using Sh = WsortShape<4>;
+            const int grid = grid_for(n, Sh::kWarps, sms * 8);
+            if (g.N <= (1 << (32 - Sh::kIdBits))) {
+                k_wsort_rows<4, true, T, unsigned>
+                    <<<grid, Sh::kThreads, Sh::smem<true, T, unsigned>(), s>>>(g, list, &h->info->counts[c]);
+            } else {
+                k_wsort_rows<4, true, T, unsigned long long>
+                    <<<grid, Sh::kThreads, Sh::smem<true, T, unsigned long long>(), s>>>(g, list, &h->info->counts[c]);
+            }
+            break;
         }
+        case kClsE1: {
+            // the staged rows (at most kE1OnePassFlopMax products, not column-window rows)
+            // by warp sort into the staging area; the rest counted by the warp hash on an
+            // extra stream
+            int *one = xl + kXlE1One * M;
+            int *two = xl + kXlE1Two * M;
+            k_split_list<2, PickStaged><<<grid_for(n, 256, sms * 4), 256, 0, s>>>(
+                list, &h->info->counts[c], PickStaged{h->soff}, one, (int)M, h->info->split1);
+            OPS_CUDA(h, cudaGetLastError());
+            ++h->launches;
+            OPS_CUDA(h, cudaEventRecord(h->ev_x_fork[0], s));
+            OPS_CUDA(h, cudaStreamWaitEvent(h->side_x[0], h->ev_x_fork[0], 0));
+            SpgemmArgs<double> gc{};
+            gc.arpt = g.arpt;
+            gc.acol = g.acol;
+            gc.brpt = g.brpt;
+            gc.bcol = g.bcol;
+            gc.M = g.M;
+            gc.K = g.K;
+            gc.N = g.N;
+            gc.row_flop = g.row_flop;
+            gc.c_rpt = g.c_rpt;
+            gc.info = g.info;
+            k_warp_rows<false, double, 2 * kEsc1FlopMax>
+                <<<grid_for(n, kWarpRowsThreads / 32, sms * 3), kWarpRowsThreads,
+                   warp_rows_smem<false, double, 2 * kEsc1FlopMax>(), h->side_x[0]>>>(gc, two, &h->info->split1[1]);
+            OPS_CUDA(h, cudaGetLastError());
+            ++h->launches;
+            OPS_CUDA(h, cudaEventRecord(h->ev_x_join[0], h->side_x[0]));
+            using Sh = WsortShape<16>;
+            const int sgrid = grid_for(n, Sh::kWarps, sms * 4);
+            if (g.N <= (1 << (32 - Sh::kIdBits))) {
+                k_wsort_rows<16, true, T, unsigned>
+                    <<<sgrid, Sh::kThreads, Sh::smem<true, T, unsigned>(), s>>>(g, one, &h->info->split1[0]);
+            } else {
+                k_wsort_rows<16, true, T, unsigned long long>
+                    <<<sgrid, Sh::kThreads, Sh::smem<true, T, unsigned long long>(), s>>>(g, one, &h->info->split1[0]);
+            }
+            OPS_CUDA(h, cudaGetLastError());
+            OPS_CUDA(h, cudaStreamWaitEvent(s, h->ev_x_join[0], 0));
+            break;
+        }
+        case kClsE2: {
+            // the counting phase's split and longest-first orders, then both numeric shapes
+            int *mid_list = xl + kXlE2Mid * M;
+            int *large_list = xl + kXlE2Large * M;
+            k_split_list<2, PickE2><<<grid_for(n, 256, sms * 4), 256, 0, s>>>(
+                list, &h->info->counts[c], PickE2{g.arpt, g.row_flop}, mid_list, (int)M, h->info->split2);
+            OPS_CUDA(h, cudaGetLastError());
+            ++h->launches;
+            OPS_CUDA(h, cudaEventRecord(h->ev_x_fork[1], s));
+            OPS_CUDA(h, cudaStreamWaitEvent(h->side_x[1], h->ev_x_fork[1], 0));
+            if (n > 1) {
+                k_sort_heavy_first<<<1, 1024, 0, h->side_x[1]>>>(large_list, &h->info->split2[1], h->row_flop);
+                OPS_CUDA(h, cudaGetLastError());
+                ++h->launches;
+            }
+            k_esc_rows<EscLarge, true, T><<<std::min(n, sms), EscLarge::kThreads, EscLarge::kNumericSmem,
+                                            h->side_x[1]>>>(g, large_list, &h->info->split2[1], &h->info->next[0][c]);
+            OPS_CUDA(h, cudaGetLastError());
+            ++h->launches;
+            OPS_CUDA(h, cudaEventRecord(h->ev_x_join[1], h->side_x[1]));
+            if (n > 1) {
+                k_sort_heavy_first<<<1, 1024, 0, s>>>(mid_list, &h->info->split2[0], h->row_flop);
+                OPS_CUDA(h, cudaGetLastError());
+                ++h->launches;
+            }
+            launch_besc<BescMid, true, T>(g, mid_list, &h->info->split2[0], &h->info->next_mid[0],
+                                          std::min(n, sms * 4), s);
+            OPS_CUDA(h, cudaGetLastError());
+            OPS_CUDA(h, cudaStreamWaitEvent(s, h->ev_x_join[1], 0));
+            break;
+        }
+        default:
+            return fail(h, OPS_NOT_SUPPORTED, "class without a one-pass kernel");
     }
+    return OPS_OK;
 }
 
-// One-pass set-up, once the class sizes are known: lays out (and grows) the staging area
-// of the R16, R32 and W rows.  Leaves h->staged false — two passes — when the call has no
-// values yet, one-pass is off, no row is in those classes, or the area would exceed the
-// handle's staging budget.
-int prepare_stage(ops_handle_s *h, cudaStream_t st)
+// One-pass set-up, once the class sizes are known: when the call has its values, one
+// pass is on and the staged products fit the handle's staging budget, grows the staging
+// area and turns the per-row product counts (k_setup's sflop) into staging offsets.
+// Otherwise leaves h->staged false: two passes.
+int prepare_stage(ops_handle_s *h, const DevInfo &hi, int M, cudaStream_t st)
 {
     h->staged = false;
     const int vs = h->op_dtype == OPS_F64 ? 8 : (h->op_dtype == OPS_F32 ? 4 : 0);
-    if (!h->one_pass || vs == 0) return OPS_OK;
-    size_t total = 0;
-    int rows = 0;
-    for (int c = 0; c < kNumClasses; ++c) {
-        const size_t slots = (size_t)h->counts[c] * (size_t)stage_cap_of(c);
-        h->stage_off[c] = total;
-        total += align_up(sizeof(int) * slots, 256) + align_up((size_t)vs * slots, 256);
-        if (stage_cap_of(c)) rows += h->counts[c];
-    }
-    if (rows == 0 || total > h->stage_budget) return OPS_OK;
+    if (!h->one_pass || vs == 0 || M == 0 || hi.staged_flop == 0) return OPS_OK;
+    if (h->one_pass == 1 && hi.staged_flop < kMinStageFlop) return OPS_OK;
+    const unsigned long long entries = hi.staged_flop;
+    const size_t total = align_up(sizeof(int) * (size_t)entries, 256) + align_up((size_t)vs * (size_t)entries, 256);
+    if (entries > (unsigned long long)INT_MAX || total > h->stage_budget) return OPS_OK;
     if (total > h->stage_bytes) {
         if (h->stage) OPS_CUDA(h, cudaFreeAsync(h->stage, st));
         h->stage = nullptr;
@@ -244,7 +336,12 @@ int prepare_stage(ops_handle_s *h, cudaStream_t st)
         h->stage = static_cast<unsigned char *>(p);
         h->stage_bytes = total;
     }
+    h->stage_entries = (long long)entries;
+    size_t cb = h->cub_bytes;
+    OPS_CUDA(h, cub::DeviceScan::ExclusiveSum(h->cub_tmp, cb, h->soff, h->soff, M + 1, st));
+    ++h->launches;
     h->staged = true;
+    h->stage_e1 = hi.e1_one > 0;
     return OPS_OK;
 }
 
@@ -271,11 +368,31 @@ int launch_classes(ops_handle_s *h, const SpgemmArgs<T> &g, cudaStream_t st)
     // heaviest classes first: their long kernels then overlap the light classes instead
     // of forming the tail of the phase
     constexpr int kOrder[kNumClasses] = {kClsE2, kClsD, kClsE1, kClsW, kClsR32, kClsR16, kClsR8};
+    if (kNum && h->staged) {
+        // one-pass call: the rows computed in the counting phase move from the staging
+        // area into C, on the caller's stream while the remaining classes run on theirs
+        k_place_staged<T><<<grid_for(g.M, 256, sms * 8), 256, 0, st>>>(
+            g.M, h->soff, g.c_rpt, g.row_flop, kEsc1FlopMax, reinterpret_cast<const int *>(h->stage),
+            stage_vals<T>(h), g.c_col, g.c_val);
+        OPS_CUDA(h, cudaGetLastError());
+        ++h->launches;
+        if (h->counts[kClsE2] > 0) {  // rows above kEsc1FlopMax products: the E2 class
+            k_place_long<T><<<std::min(h->counts[kClsE2], sms * 8), 256, 0, st>>>(
+                h->lists + (size_t)kClsE2 * M, &h->info->counts[kClsE2], h->soff, g.c_rpt,
+                reinterpret_cast<const int *>(h->stage), stage_vals<T>(h), g.c_col, g.c_val);
+            OPS_CUDA(h, cudaGetLastError());
+            ++h->launches;
+        }
+    }
     for (int oi = 0; oi < kNumClasses; ++oi) {
         const int c = kOrder[oi];
         const int n = h->counts[c];
         if (n <= 0) continue;
-        if (!kNum && c == kClsR8) continue;  // R8 rows are counted inside k_setup
+        const bool staged = h->staged && staged_class(h, c);
+        // R8 rows are counted inside k_setup; staged classes are done after the counting
+        // phase, except the E1 rows left to two passes
+        if (!kNum && c == kClsR8 && !staged) continue;
+        if (kNum && staged && c != kClsE1) continue;
         cudaStream_t s = h->side[c];
         OPS_CUDA(h, cudaStreamWaitEvent(s, h->ev_fork, 0));
         const int *list = h->lists + (size_t)c * M;
@@ -286,15 +403,9 @@ int launch_classes(ops_handle_s *h, const SpgemmArgs<T> &g, cudaStream_t st)
             ++h->launches;
         }
         if (h->timing >= 2) OPS_CUDA(h, cudaEventRecord(h->ev_k[kNum][c][0], s));
-        const bool staged = h->staged && stage_cap_of(c) > 0;
         if (staged && !kNum) {  // one-pass call: numeric into the staging area
-            if (h->op_dtype == OPS_F64) launch_staged_numeric<double>(h, g, c, list, n, s);
-            else launch_staged_numeric<float>(h, g, c, list, n, s);
-        } else if (staged) {    // ... and its placement into C
-            const int cap = stage_cap_of(c);
-            k_place_staged<T><<<grid_for((long long)n * cap, 256, sms * 8), 256, 0, s>>>(
-                list, n, ceil_log2(cap), reinterpret_cast<const int *>(h->stage + h->stage_off[c]),
-                stage_vals<T>(h, c, n), g.c_rpt, g.c_col, g.c_val);
+            OPS_CHECK(h->op_dtype == OPS_F64 ? launch_staged_class<double>(h, g, c, list, n, s)
+                                             : launch_staged_class<float>(h, g, c, list, n, s));
         } else
         switch (c) {
             case kClsR8:  // numeric only: walks the rows in order
@@ -330,12 +441,15 @@ int launch_classes(ops_handle_s *h, const SpgemmArgs<T> &g, cudaStream_t st)
                     break;
                 }
                 // re-bin by output size: warp sort / warp hash on this stream,
-                // expand/sort/compress on an extra stream
+                // expand/sort/compress on an extra stream (a one-pass call re-bins only
+                // the rows it left to two passes)
                 int *sort_list = xl + kXlE1Sort * M;
                 int *hash_list = xl + kXlE1Hash * M;
                 int *esc_list = xl + kXlE1Esc * M;
+                const int *e1_list = staged ? xl + kXlE1Two * M : list;
+                const int *e1_count = staged ? &h->info->split1[1] : &h->info->counts[c];
                 k_split_list<3, PickE1><<<grid_for(n, 256, sms * 4), 256, 0, s>>>(
-                    list, &h->info->counts[c], PickE1{g.c_rpt, g.row_flop, kWsortFlopMax}, sort_list, (int)M,
+                    e1_list, e1_count, PickE1{g.c_rpt, g.row_flop, kWsortFlopMax}, sort_list, (int)M,
                     h->info->split);
                 OPS_CUDA(h, cudaGetLastError());
                 ++h->launches;
@@ -461,10 +575,15 @@ int run_symbolic(ops_handle_s *h, const Mat &A, const Mat &B, int *c_rpt, long l
     if (h->timing) OPS_CUDA(h, cudaEventRecord(h->ev_t[0], st));
     OPS_CUDA(h, cudaMemsetAsync(h->info, 0, sizeof(DevInfo), st));
     OPS_CUDA(h, cudaMemsetAsync(c_rpt + M, 0, sizeof(int), st));
+    // a one-pass call also gets the per-row products it may stage (made into offsets once
+    // the staging area is known to fit)
+    const bool want_stage = h->one_pass != 0 && h->op_dtype >= 0;
+    if (want_stage) OPS_CUDA(h, cudaMemsetAsync(h->soff + M, 0, sizeof(int), st));
     if (h->timing) OPS_CUDA(h, cudaEventRecord(h->ev_t[1], st));
     if (M > 0) {
         k_setup<<<(M + kSetupThreads - 1) / kSetupThreads, kSetupThreads, 0, st>>>(
-            A.rpt, A.col, B.rpt, B.col, M, A.cols, B.cols, h->row_flop, h->lists, c_rpt, h->info, h->th);
+            A.rpt, A.col, B.rpt, B.col, M, A.cols, B.cols, h->row_flop, h->lists, c_rpt,
+            want_stage ? h->soff : nullptr, h->info, h->th);
         OPS_CUDA(h, cudaGetLastError());
         ++h->launches;
     }
@@ -483,7 +602,8 @@ int run_symbolic(ops_handle_s *h, const Mat &A, const Mat &B, int *c_rpt, long l
     h->plan_flop = (long long)hi.total_flop;
     h->plan_d_flop = (long long)hi.d_flop;
     h->plan_d_len_a = (long long)hi.d_len_a;
-    OPS_CHECK(prepare_stage(h, st));
+    h->staged = false;
+    if (want_stage) OPS_CHECK(prepare_stage(h, hi, M, st));
 
     SpgemmArgs<double> g{};
     g.arpt = A.rpt;
@@ -748,10 +868,10 @@ int ops_handle_get_thresholds(ops_handle_t h, int32_t *th, int n)
     return OPS_OK;
 }
 
-int ops_handle_set_one_pass(ops_handle_t h, int enable)
+int ops_handle_set_one_pass(ops_handle_t h, int mode)
 {
-    if (!h) return OPS_INVALID_ARGUMENT;
-    h->one_pass = enable != 0;
+    if (!h || mode < 0 || mode > 2) return OPS_INVALID_ARGUMENT;
+    h->one_pass = mode;
     return OPS_OK;
 }
 
@@ -773,7 +893,7 @@ int ops_handle_subclass_rows(ops_handle_t h, int32_t *out, int n)
     if (h->info) {
         DevInfo d{};
         OPS_CUDA(h, cudaMemcpy(&d, h->info, sizeof(DevInfo), cudaMemcpyDeviceToHost));
-        v[0] = d.split[0];
+        v[0] = d.split[0] + d.split1[0];  // a one-pass call sorts its lighter E1 rows while counting
         v[1] = d.split[1];
         v[2] = d.split[2];
         v[3] = d.split2[0];

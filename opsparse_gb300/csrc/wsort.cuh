@@ -18,6 +18,7 @@
 namespace opsg {
 
 constexpr int kWsortFlopMax = 512;  // largest row of the 16-per-lane variant
+static_assert(kE1OnePassFlopMax <= kWsortFlopMax, "one-pass E1 rows use the warp sort");
 
 // Shared-memory index of element e with one pad word per 32: the blocked register layout
 // (lane l holds elements l*PER .. l*PER+PER-1) then reads and writes without bank
@@ -148,8 +149,8 @@ __global__ void __launch_bounds__(WsortShape<PMAX>::kThreads, WsortShape<PMAX>::
         long long off = 0;
         int n_expect = 0;
         if constexpr (kNum) {
-            if (g.stage_cap) {  // one-pass: the list entry's staging slot, count unknown
-                off = it * g.stage_cap;
+            if (g.soff) {  // one-pass: the row's staging slot, count unknown
+                off = __ldg(g.soff + r);
                 n_expect = INT_MAX;
             } else {
                 off = __ldg(g.c_rpt + r);
@@ -237,7 +238,7 @@ __global__ void __launch_bounds__(WsortShape<PMAX>::kThreads, WsortShape<PMAX>::
                 }
             }
         }
-        if (!kNum || g.stage_cap) {
+        if (!kNum || g.soff) {
             if (lane == 0) {
                 g.c_rpt[r] = total;
                 nnz_acc += (unsigned long long)total;
@@ -247,7 +248,7 @@ __global__ void __launch_bounds__(WsortShape<PMAX>::kThreads, WsortShape<PMAX>::
         }
         __syncwarp();
     }
-    if (!kNum || g.stage_cap) warp_add_u64(nnz_acc, &g.info->total_nnz);
+    if (!kNum || g.soff) warp_add_u64(nnz_acc, &g.info->total_nnz);
 }
 
 }  // namespace opsg

@@ -70,12 +70,13 @@ def test_f32(cuda, handle, case):
     assert np.all(val[~nz] == 0)
 
 
-@pytest.mark.parametrize("one_pass", [True, False], ids=["one_pass", "two_pass"])
+@pytest.mark.parametrize("one_pass", [2, 0], ids=["one_pass", "two_pass"])
 @pytest.mark.parametrize("dtype", ["f64", "f32"])
 @pytest.mark.parametrize("case", CASES, ids=IDS)
 def test_oneshot_against_oracle(cuda, case, dtype, one_pass):
-    """ops_spgemm (values known before counting, so rows of at most 128 products may run
-    in one pass through the staging area) is bit-identical to the oracle either way."""
+    """ops_spgemm (values known before counting, so all rows but the heaviest may be
+    computed in one pass through the staging area) is bit-identical to the oracle either
+    way; mode 2 stages even these small inputs."""
     name, a, b, ncols = case
     npd = np.float64 if dtype == "f64" else np.float32
     a = (a[0], a[1], a[2].astype(npd))
@@ -176,6 +177,29 @@ def test_wide_columns(cuda, handle, dtype):
     assert np.array_equal(rpt.astype(np.int64), orpt)
     assert np.array_equal(col, f(ocol))
     assert handle.subclass_rows()["e1_sort"] > 0
+
+
+@pytest.mark.parametrize("dtype", ["f64", "f32"])
+def test_wide_columns_one_pass(cuda, dtype):
+    """The one-pass kernels with 64-bit (column, product) keys: ops_spgemm on more than
+    2^25 columns, staged at any size, gives the oracle's bits under the column map."""
+    case, f = _stretch_columns(CASES[2])
+    name, a, b, ncols = case
+    orig = CASES[2]
+    npd = np.float64 if dtype == "f64" else np.float32
+    a = (a[0], a[1], a[2].astype(npd))
+    b = (b[0], b[1], b[2].astype(npd))
+    with ops.Handle() as h:
+        h.set_one_pass(2)
+        rpt, col, val = run_case(cuda, h, (name, a, b, ncols), getattr(cuda, "float64" if dtype == "f64" else
+                                                                       "float32"), oneshot=True)
+        orpt, ocol, oval = oracle.spgemm(orig[1][0], orig[1][1], a[2], orig[2][0], orig[2][1], b[2], orig[3],
+                                         dtype=npd)
+        ut = np.uint64 if dtype == "f64" else np.uint32
+        assert np.array_equal(rpt.astype(np.int64), orpt)
+        assert np.array_equal(col, f(ocol))
+        assert np.array_equal(val.view(ut), oval.view(ut))
+        assert h.subclass_rows()["e1_sort"] > 0
 
 
 def test_many_d_rows_wide(cuda, handle):
