@@ -28,8 +28,9 @@ enum RowClass : int {
 
 // Extra device lists after the kNumClasses class lists: the numeric re-binning of the E1
 // rows and the size split of the E2 rows.
-// The last two split the E1 rows of a one-pass call into those computed in the counting
-// phase and those left to two passes.
+// The last three split the E1 rows of a one-pass call into those computed in the
+// counting phase (by warp sort, or expand/sort/compress above kE1OnePassFlopMax products)
+// and those left to two passes.
 enum : int {
     kXlE1Sort = 0,
     kXlE1Hash = 1,
@@ -38,7 +39,8 @@ enum : int {
     kXlE2Large = 4,
     kXlE1One = 5,
     kXlE1Two = 6,
-    kNumExtraLists = 7
+    kXlE1OneLarge = 7,
+    kNumExtraLists = 8
 };
 constexpr int kNumLists = kNumClasses + kNumExtraLists;
 
@@ -48,8 +50,8 @@ constexpr int kEsc1FlopMax = 1024;
 constexpr int kEsc1AMax = 1024;
 constexpr int kEsc2FlopMax = 13312;
 constexpr int kEsc2AMax = 2560;
-// E1 rows computed in the counting phase of a one-pass call (warp sort of at most this
-// many products); heavier E1 rows keep two passes, and so do column-window rows (below)
+// E1 rows computed in the counting phase of a one-pass call: by warp sort up to this many
+// products, by CTA expand/sort/compress above; column-window rows (below) keep two passes
 constexpr int kE1OnePassFlopMax = 512;
 // Column-window rows: rows whose B rows are long (at least 16 products per A entry) and
 // whose products all fall within kWinBits consecutive columns (banded and stencil
@@ -89,7 +91,7 @@ struct DevInfo {
     int split[3];                 // E1 rows re-binned for the numeric phase: [warp sort, hash, expand/sort]
     int split2[2];                // E2 rows by size, fixed at the symbolic phase: [mid shape, large shape]
     int next_mid[2];              // row cursor of the mid-shape E2 kernel [symbolic, numeric]
-    int split1[2];                // E1 rows of a one-pass call: [one pass (flop <= kWsortFlopMax), two passes]
+    int split1[3];                // E1 rows of a one-pass call: [warp sort, two passes, expand/sort/compress]
     unsigned long long staged_flop;  // products of the rows a one-pass call may stage
     int e1_one;                   // E1 rows a one-pass call may stage
     unsigned long long d_len_a;   // A entries of the D rows

@@ -481,10 +481,16 @@ struct PickE1 {
     }
 };
 
-// Rows of a one-pass call: 0 = staged (a staging slot of one or more products), 1 = not.
+// E1 rows of a one-pass call: 0 = staged (a staging slot of one or more products) with at
+// most kE1OnePassFlopMax products, 1 = not staged, 2 = staged with more products.
 struct PickStaged {
     const int *soff;
-    __device__ int operator()(int r) const { return soff[r + 1] > soff[r] ? 0 : 1; }
+    const int *row_flop;
+    __device__ int operator()(int r) const
+    {
+        if (soff[r + 1] <= soff[r]) return 1;
+        return row_flop[r] <= kE1OnePassFlopMax ? 0 : 2;
+    }
 };
 
 // E2 rows by size: 0 = mid shape (EscMid), 1 = large shape (EscLarge).

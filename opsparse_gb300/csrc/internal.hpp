@@ -77,6 +77,7 @@ struct ops_handle_s {
     const void *op_aval = nullptr, *op_bval = nullptr;
     bool staged = false;           // the counting phase of the call in progress stages
     bool stage_e1 = false;         // ... and some of its rows are E1 rows
+    bool stage_e1_all = false;     // ... all of the E1 rows
     unsigned char *stage = nullptr;        // [columns | values] of stage_entries entries
     size_t stage_bytes = 0;
     long long stage_entries = 0;

@@ -282,10 +282,10 @@ static __global__ void __launch_bounds__(kSetupThreads) k_setup(const int *__res
     // the heavier E1 rows), for the prefix that places them in the staging area
     int staged = 0;
     if (sflop) {
-        staged = (cls >= 0 && cls != kClsD && (cls != kClsE1 || f32 <= kE1OnePassFlopMax)) ? f32 : 0;
-        if (cls == kClsE1 && staged && f32 >= 16 * lenA) {
+        staged = (cls >= 0 && cls != kClsD) ? f32 : 0;
+        if (cls == kClsE1 && f32 >= 16 * lenA) {
             // a column-window row keeps two passes: span of its B rows' first and last
-            // columns (B rows are sorted; lenA <= 32 here)
+            // columns (B rows are sorted; lenA <= 64 here)
             int cmin = INT_MAX, cmax = -1;
             if (light) {
 #pragma unroll
@@ -550,112 +550,100 @@ __global__ void __launch_bounds__(256) k_reg_rows(SpgemmArgs<T> g, const int *__
     if (!kNum || g.soff) warp_add_u64(nnz_acc, &g.info->total_nnz);
 }
 
-// Moves the staged rows of a one-pass call into C, in row order: row r was staged if
-// soff[r + 1] > soff[r] (its staging slot holds up to its product count), and its
-// c_rpt[r + 1] - c_rpt[r] entries go to C from c_rpt[r] on.  A warp takes 32 consecutive
-// rows and walks the concatenation of their entries 32 at a time, each lane finding the
-// row of its entry by a binary search over the warp's prefix of counts, with kPlaceUnroll
-// chunks' loads in flight together: C is written contiguously and the staging area read
-// almost so (its slots follow row order).
-constexpr int kPlaceUnroll = 4;
+// Moves the staged rows of a one-pass call into C.  Row r was staged if soff[r + 1] >
+// soff[r] (its staging slot holds up to its product count); its c_rpt[r + 1] - c_rpt[r]
+// entries go to C from c_rpt[r] on.  C's entries are cut into ranges of kPlaceRange; a
+// warp finds the row holding its range's first entry by a 32-way search of c_rpt (four
+// rounds of one load per lane for a million rows), then takes 32 rows at a time and walks
+// the concatenation of their entries inside the range, each lane locating its entry's row
+// by a binary search over the warp's prefix of counts, kPlaceUnroll chunks' loads in
+// flight together.  Every warp copies about the same number of entries, however the row
+// lengths are spread; C is written contiguously and the staging area read almost so (its
+// slots follow row order).
+constexpr int kPlaceUnroll = 8;
+constexpr int kPlaceRange = 1024;
 
-// Rows of more than long_flop products are skipped here and copied by k_place_long, so
-// that no warp is left with a long serial copy.
 template <typename T>
 __global__ void __launch_bounds__(256) k_place_staged(int M, const int *__restrict__ soff,
-                                                      const int *__restrict__ c_rpt, const int *__restrict__ row_flop,
-                                                      int long_flop, const int *__restrict__ scol,
+                                                      const int *__restrict__ c_rpt, const int *__restrict__ scol,
                                                       const T *__restrict__ sval, int *__restrict__ c_col,
                                                       T *__restrict__ c_val)
 {
     const int lane = lane_id();
     const long long warp0 = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
-    for (long long w = warp0; w * 32 < M; w += nwarps) {
-        const int r = (int)(w * 32) + lane;
-        int so = 0, o = 0, n = 0;
-        if (r < M) {
-            so = __ldg(soff + r);
-            if (__ldg(soff + r + 1) > so && __ldg(row_flop + r) <= long_flop) {
+    const int nnz = __ldg(c_rpt + M);
+    for (long long q = warp0; q * kPlaceRange < nnz; q += nwarps) {
+        const int p0 = (int)(q * kPlaceRange);
+        const int p1 = min(nnz, p0 + kPlaceRange);
+        // row of entry p0: c_rpt[lo] <= p0 < c_rpt[hi]
+        int lo = 0, hi = M;
+        while (hi - lo > 1) {
+            const int step = (hi - lo + 31) / 32;
+            const long long idx = (long long)lo + (long long)(lane + 1) * step;
+            const int v = idx < hi ? __ldg(c_rpt + idx) : INT_MAX;
+            const int k = __popc(__ballot_sync(kFull, v <= p0));
+            const int nlo = lo + k * step;
+            hi = (int)min((long long)hi, (long long)nlo + step);
+            lo = nlo;
+        }
+        for (int r0 = lo; r0 < M; r0 += 32) {
+            const int r = r0 + lane;
+            int so = 0, o = 0, o1 = 0, n = 0, src0 = 0, dst0 = 0;
+            if (r < M) {  // the row's four words are loaded together
+                so = __ldg(soff + r);
+                const int so1 = __ldg(soff + r + 1);
                 o = __ldg(c_rpt + r);
-                n = __ldg(c_rpt + r + 1) - o;
-            }
-        }
-        int incl = n;
-#pragma unroll
-        for (int d = 1; d < 32; d <<= 1) {
-            const int t = __shfl_up_sync(kFull, incl, d);
-            if (lane >= d) incl += t;
-        }
-        const int total = __shfl_sync(kFull, incl, 31);
-        for (int base = 0; base < total; base += 32 * kPlaceUnroll) {
-            int src[kPlaceUnroll], dst[kPlaceUnroll];
-#pragma unroll
-            for (int u = 0; u < kPlaceUnroll; ++u) {
-                const int e = base + u * 32 + lane;
-                int lo = 0;  // lanes whose rows end at or before entry e
-#pragma unroll
-                for (int step = 16; step >= 1; step >>= 1) {
-                    const int v = __shfl_sync(kFull, incl, lo + step - 1);
-                    if (v <= e) lo += step;
-                }
-                const int l = min(lo, 31);
-                const int first = __shfl_sync(kFull, incl, l) - __shfl_sync(kFull, n, l);
-                const int s0 = __shfl_sync(kFull, so, l);
-                const int o0 = __shfl_sync(kFull, o, l);
-                src[u] = e < total ? s0 + (e - first) : -1;
-                dst[u] = o0 + (e - first);
-            }
-            int cv[kPlaceUnroll];
-            T vv[kPlaceUnroll];
-#pragma unroll
-            for (int u = 0; u < kPlaceUnroll; ++u) {
-                cv[u] = src[u] >= 0 ? __ldg(scol + src[u]) : 0;
-                vv[u] = src[u] >= 0 ? __ldg(sval + src[u]) : T(0);
-            }
-#pragma unroll
-            for (int u = 0; u < kPlaceUnroll; ++u) {
-                if (src[u] >= 0) {
-                    c_col[dst[u]] = cv[u];
-                    c_val[dst[u]] = vv[u];
+                o1 = __ldg(c_rpt + r + 1);
+                const int e0 = max(o, p0), e1 = min(o1, p1);
+                if (so1 > so && e1 > e0) {
+                    n = e1 - e0;
+                    src0 = so + (e0 - o);
+                    dst0 = e0;
                 }
             }
-        }
-    }
-}
-
-// The long staged rows (a class list): one CTA per row, kPlaceUnroll entries per thread
-// in flight.
-template <typename T>
-__global__ void __launch_bounds__(256) k_place_long(const int *__restrict__ list, const int *count_ptr,
-                                                    const int *__restrict__ soff, const int *__restrict__ c_rpt,
-                                                    const int *__restrict__ scol, const T *__restrict__ sval,
-                                                    int *__restrict__ c_col, T *__restrict__ c_val)
-{
-    const int count = *count_ptr;
-    for (int i = blockIdx.x; i < count; i += gridDim.x) {
-        const int r = __ldg(list + i);
-        const int so = __ldg(soff + r);
-        if (__ldg(soff + r + 1) <= so) continue;  // not staged (block-uniform)
-        const int o = __ldg(c_rpt + r);
-        const int n = __ldg(c_rpt + r + 1) - o;
-        for (int base = 0; base < n; base += kPlaceUnroll * (int)blockDim.x) {
-            int cv[kPlaceUnroll];
-            T vv[kPlaceUnroll];
+            int incl = n;
 #pragma unroll
-            for (int u = 0; u < kPlaceUnroll; ++u) {
-                const int e = base + u * (int)blockDim.x + (int)threadIdx.x;
-                cv[u] = e < n ? __ldg(scol + so + e) : 0;
-                vv[u] = e < n ? __ldg(sval + so + e) : T(0);
+            for (int d = 1; d < 32; d <<= 1) {
+                const int t = __shfl_up_sync(kFull, incl, d);
+                if (lane >= d) incl += t;
             }
+            const int total = __shfl_sync(kFull, incl, 31);
+            for (int base = 0; base < total; base += 32 * kPlaceUnroll) {
+                int src[kPlaceUnroll], dst[kPlaceUnroll];
 #pragma unroll
-            for (int u = 0; u < kPlaceUnroll; ++u) {
-                const int e = base + u * (int)blockDim.x + (int)threadIdx.x;
-                if (e < n) {
-                    c_col[o + e] = cv[u];
-                    c_val[o + e] = vv[u];
+                for (int u = 0; u < kPlaceUnroll; ++u) {
+                    const int e = base + u * 32 + lane;
+                    int l = 0;  // lanes whose entries end at or before e
+#pragma unroll
+                    for (int step = 16; step >= 1; step >>= 1) {
+                        const int v = __shfl_sync(kFull, incl, l + step - 1);
+                        if (v <= e) l += step;
+                    }
+                    l = min(l, 31);
+                    const int first = __shfl_sync(kFull, incl, l) - __shfl_sync(kFull, n, l);
+                    const int s0 = __shfl_sync(kFull, src0, l);
+                    const int d0 = __shfl_sync(kFull, dst0, l);
+                    src[u] = e < total ? s0 + (e - first) : -1;
+                    dst[u] = d0 + (e - first);
+                }
+                int cv[kPlaceUnroll];
+                T vv[kPlaceUnroll];
+#pragma unroll
+                for (int u = 0; u < kPlaceUnroll; ++u) {
+                    cv[u] = src[u] >= 0 ? __ldg(scol + src[u]) : 0;
+                    vv[u] = src[u] >= 0 ? __ldg(sval + src[u]) : T(0);
+                }
+#pragma unroll
+                for (int u = 0; u < kPlaceUnroll; ++u) {
+                    if (src[u] >= 0) {
+                        c_col[dst[u]] = cv[u];
+                        c_val[dst[u]] = vv[u];
+                    }
                 }
             }
+            // done once this window of rows reaches the end of the range
+            if (__shfl_sync(kFull, r < M ? o1 : INT_MAX, 31) >= p1) break;
         }
     }
 }

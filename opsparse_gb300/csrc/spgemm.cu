@@ -233,17 +233,22 @@ int launch_staged_class(ops_handle_s *h, const GA &gs, int c, const int *list, i
             break;
         }
         case kClsE1: {
-            // the staged rows (at most kE1OnePassFlopMax products, not column-window rows)
-            // by warp sort into the staging area; the rest counted by the warp hash on an
-            // extra stream
+            // the staged rows (not column-window rows) into the staging area: by warp sort
+            // up to kE1OnePassFlopMax products, else (on an extra stream) by CTA
+            // expand/sort/compress; the rest counted by the warp hash
             int *one = xl + kXlE1One * M;
             int *two = xl + kXlE1Two * M;
-            k_split_list<2, PickStaged><<<grid_for(n, 256, sms * 4), 256, 0, s>>>(
-                list, &h->info->counts[c], PickStaged{h->soff}, one, (int)M, h->info->split1);
+            int *one_large = xl + kXlE1OneLarge * M;
+            k_split_list<3, PickStaged><<<grid_for(n, 256, sms * 4), 256, 0, s>>>(
+                list, &h->info->counts[c], PickStaged{h->soff, g.row_flop}, one, (int)M, h->info->split1);
             OPS_CUDA(h, cudaGetLastError());
             ++h->launches;
             OPS_CUDA(h, cudaEventRecord(h->ev_x_fork[0], s));
             OPS_CUDA(h, cudaStreamWaitEvent(h->side_x[0], h->ev_x_fork[0], 0));
+            launch_besc<BescE1, true, T>(g, one_large, &h->info->split1[2], &h->info->next[0][c],
+                                         std::min(n, sms * 8), h->side_x[0]);
+            OPS_CUDA(h, cudaGetLastError());
+            ++h->launches;
             SpgemmArgs<double> gc{};
             gc.arpt = g.arpt;
             gc.acol = g.acol;
@@ -342,6 +347,7 @@ int prepare_stage(ops_handle_s *h, const DevInfo &hi, int M, cudaStream_t st)
     ++h->launches;
     h->staged = true;
     h->stage_e1 = hi.e1_one > 0;
+    h->stage_e1_all = hi.e1_one == hi.counts[kClsE1];
     return OPS_OK;
 }
 
@@ -371,18 +377,11 @@ int launch_classes(ops_handle_s *h, const SpgemmArgs<T> &g, cudaStream_t st)
     if (kNum && h->staged) {
         // one-pass call: the rows computed in the counting phase move from the staging
         // area into C, on the caller's stream while the remaining classes run on theirs
-        k_place_staged<T><<<grid_for(g.M, 256, sms * 8), 256, 0, st>>>(
-            g.M, h->soff, g.c_rpt, g.row_flop, kEsc1FlopMax, reinterpret_cast<const int *>(h->stage),
-            stage_vals<T>(h), g.c_col, g.c_val);
+        const long long ranges = (h->plan_nnz + kPlaceRange - 1) / kPlaceRange;
+        k_place_staged<T><<<grid_for(ranges, 8, sms * 8), 256, 0, st>>>(
+            g.M, h->soff, g.c_rpt, reinterpret_cast<const int *>(h->stage), stage_vals<T>(h), g.c_col, g.c_val);
         OPS_CUDA(h, cudaGetLastError());
         ++h->launches;
-        if (h->counts[kClsE2] > 0) {  // rows above kEsc1FlopMax products: the E2 class
-            k_place_long<T><<<std::min(h->counts[kClsE2], sms * 8), 256, 0, st>>>(
-                h->lists + (size_t)kClsE2 * M, &h->info->counts[kClsE2], h->soff, g.c_rpt,
-                reinterpret_cast<const int *>(h->stage), stage_vals<T>(h), g.c_col, g.c_val);
-            OPS_CUDA(h, cudaGetLastError());
-            ++h->launches;
-        }
     }
     for (int oi = 0; oi < kNumClasses; ++oi) {
         const int c = kOrder[oi];
@@ -392,7 +391,7 @@ int launch_classes(ops_handle_s *h, const SpgemmArgs<T> &g, cudaStream_t st)
         // R8 rows are counted inside k_setup; staged classes are done after the counting
         // phase, except the E1 rows left to two passes
         if (!kNum && c == kClsR8 && !staged) continue;
-        if (kNum && staged && c != kClsE1) continue;
+        if (kNum && staged && (c != kClsE1 || h->stage_e1_all)) continue;
         cudaStream_t s = h->side[c];
         OPS_CUDA(h, cudaStreamWaitEvent(s, h->ev_fork, 0));
         const int *list = h->lists + (size_t)c * M;
@@ -893,9 +892,10 @@ int ops_handle_subclass_rows(ops_handle_t h, int32_t *out, int n)
     if (h->info) {
         DevInfo d{};
         OPS_CUDA(h, cudaMemcpy(&d, h->info, sizeof(DevInfo), cudaMemcpyDeviceToHost));
-        v[0] = d.split[0] + d.split1[0];  // a one-pass call sorts its lighter E1 rows while counting
+        // a one-pass call computes its staged E1 rows while counting (split1)
+        v[0] = d.split[0] + d.split1[0];
         v[1] = d.split[1];
-        v[2] = d.split[2];
+        v[2] = d.split[2] + d.split1[2];
         v[3] = d.split2[0];
         v[4] = d.split2[1];
     }
