@@ -68,8 +68,8 @@ struct ops_handle_s {
     int dense_ctas = 0;
 
     // one-pass numeric (ops_spgemm, where the values are known before the counting
-    // phase): every row but the D rows, the E1 rows above kE1OnePassFlopMax products and
-    // the E1 column-window rows is computed in the counting phase into a staging area
+    // phase): every row but the R8 rows, the D rows and the E1 column-window rows is
+    // computed in the counting phase into a staging area
     // (grow-only) at the exclusive prefix of the staged rows' product counts, and moved
     // into C after the scan
     int one_pass = 1;              // 0 off, 1 on above kMinStageFlop staged products, 2 on

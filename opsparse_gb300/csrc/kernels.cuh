@@ -278,11 +278,12 @@ static __global__ void __launch_bounds__(kSetupThreads) k_setup(const int *__res
             if (cls == c) my_off = base + __popc(mk & lanemask_lt());
         }
     }
-    // products a one-pass call may compute in the counting phase (every class but D and
-    // the heavier E1 rows), for the prefix that places them in the staging area
+    // products a one-pass call may compute in the counting phase (every class but R8, whose
+    // count is made here and whose numeric runs straight into C, D, and the E1
+    // column-window rows), for the prefix that places them in the staging area
     int staged = 0;
     if (sflop) {
-        staged = (cls >= 0 && cls != kClsD) ? f32 : 0;
+        staged = (cls > kClsR8 && cls != kClsD) ? f32 : 0;
         if (cls == kClsE1 && f32 >= 16 * lenA) {
             // a column-window row keeps two passes: span of its B rows' first and last
             // columns (B rows are sorted; lenA <= 64 here)
@@ -428,9 +429,8 @@ __global__ void __launch_bounds__(kSmallThreads, 4) k_small_rows(SpgemmArgs<T> g
         OPSG_CS(1, 4); OPSG_CS(3, 6);
         OPSG_CS(1, 2); OPSG_CS(3, 4); OPSG_CS(5, 6);
 #undef OPSG_CS
-        // one-pass: the staging slot of the row; c_rpt[r] still holds the row's count
-        const int off = g.soff ? __ldg(g.soff + r) : __ldg(g.c_rpt + r);
-        const int n_expect = g.soff ? __ldg(g.c_rpt + r) : __ldg(g.c_rpt + r + 1) - off;
+        const int off = __ldg(g.c_rpt + r);
+        const int n_expect = __ldg(g.c_rpt + r + 1) - off;
         typename AccT::S acc = AccT::zero();
         int pos = 0;
 #pragma unroll

@@ -168,11 +168,15 @@ int grid_for(long long work_items, int per_block, int cap)
     return (int)std::max<long long>(1, std::min<long long>(b, cap));
 }
 
-// Classes whose rows a one-pass call computes in the counting phase: all but D, and E1
-// only if some E1 row is staged (at most kE1OnePassFlopMax products, not a column-window
+// Classes whose rows a one-pass call computes in the counting phase: all but R8 (counted
+// by k_setup; their numeric writes C directly in the second phase, next to the copy of the
+// staged rows) and D, and E1 only if some E1 row is staged (at most kE1OnePassFlopMax products, not a column-window
 // row; the split is made on the device, without such rows the E1 class keeps its own
 // list and two passes).
-bool staged_class(const ops_handle_s *h, int c) { return c != kClsD && (c != kClsE1 || h->stage_e1); }
+bool staged_class(const ops_handle_s *h, int c)
+{
+    return c != kClsR8 && c != kClsD && (c != kClsE1 || h->stage_e1);
+}
 
 // Below this many staged products the set-up of a one-pass call (the offset scan, the
 // copy into C) costs more than the counting kernels it saves.
@@ -211,9 +215,6 @@ int launch_staged_class(ops_handle_s *h, const GA &gs, int c, const int *list, i
     const size_t M = (size_t)h->plan_M;
     int *xl = h->lists + (size_t)kNumClasses * M;
     switch (c) {
-        case kClsR8:
-            k_small_rows<T><<<grid_for(g.M, kSmallThreads, sms * 8), kSmallThreads, 0, s>>>(g, h->plan_th.r8);
-            break;
         case kClsR16:
             k_reg_rows<16, true, T><<<grid_for((n + 1) / 2, 8, sms * 8), 256, 0, s>>>(g, list, n);
             break;
@@ -390,7 +391,7 @@ int launch_classes(ops_handle_s *h, const SpgemmArgs<T> &g, cudaStream_t st)
         const bool staged = h->staged && staged_class(h, c);
         // R8 rows are counted inside k_setup; staged classes are done after the counting
         // phase, except the E1 rows left to two passes
-        if (!kNum && c == kClsR8 && !staged) continue;
+        if (!kNum && c == kClsR8) continue;
         if (kNum && staged && (c != kClsE1 || h->stage_e1_all)) continue;
         cudaStream_t s = h->side[c];
         OPS_CUDA(h, cudaStreamWaitEvent(s, h->ev_fork, 0));
