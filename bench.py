@@ -346,23 +346,46 @@ def run_ours(args, desc, dt, data, n, rank, world, local_rank):
              torch.empty(max(nnz_c, 1), dtype=tdt).pin_memory()]
     h2d = sum(x.numel() * x.element_size() for x in pin)
     d2h = (n + 1) * 4 + nnz_c * (4 + s)
+    # host<->device copies split over several streams so that the copy engines work on
+    # them together (one stream per input array; C's columns and values in halves)
+    copy_streams = [torch.cuda.Stream(device=dev) for _ in range(4)]
+
+    def fan_out(jobs):
+        """Run copy jobs on the copy streams after the work queued so far on `stream`,
+        and make `stream` wait for all of them."""
+        start = torch.cuda.Event()
+        start.record(stream)
+        for k, job in enumerate(jobs):
+            cs = copy_streams[k % len(copy_streams)]
+            cs.wait_event(start)
+            with torch.cuda.stream(cs):
+                job()
+        for cs in copy_streams[:len(jobs)]:
+            done = torch.cuda.Event()
+            done.record(cs)
+            stream.wait_event(done)
+
+    vstr = "<f8" if dt == "f64" else "<f4"
     e2e_ms = []
     for i in range(args.warmup + args.steps):
         flush.zero_()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
-        for d, p in zip(d_in, pin):
-            d.copy_(p, non_blocking=True)
+        fan_out([lambda d=d, p=p: d.copy_(p, non_blocking=True) for d, p in zip(d_in, pin)])
         rp2, cp2, vp2 = C.c_void_p(), C.c_void_p(), C.c_void_p()
         nnz = C.c_int64(0)
         capi.check(lib.ops_spgemm(h.h, code, n, n, n, d_in[0].data_ptr(), d_in[1].data_ptr(), d_in[2].data_ptr(),
                                   A.nnz, d_b[0].data_ptr(), d_b[1].data_ptr(), d_b[2].data_ptr(), B.nnz,
                                   C.byref(rp2), C.byref(cp2), C.byref(vp2), C.byref(nnz), st), h.h)
-        vstr = "<f8" if dt == "f64" else "<f4"
+        jobs = []
         for hb, dp, cnt, ts in ((h_out[0], rp2, n + 1, "<i4"), (h_out[1], cp2, nnz_c, "<i4"),
                                 (h_out[2], vp2, nnz_c, vstr)):
             dv = torch.as_tensor(ops._DevArray(dp.value, cnt, ts), device=dev)
-            hb[:cnt].copy_(dv, non_blocking=True)
+            parts = 1 if cnt < (1 << 20) else 2
+            cuts = [cnt * k // parts for k in range(parts + 1)]
+            for a, b in zip(cuts[:-1], cuts[1:]):
+                jobs.append(lambda hb=hb, dv=dv, a=a, b=b: hb[a:b].copy_(dv[a:b], non_blocking=True))
+        fan_out(jobs)
         e1.record(stream)
         torch.cuda.synchronize()
         release((rp2, cp2, vp2))
