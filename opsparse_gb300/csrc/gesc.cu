@@ -205,16 +205,18 @@ __global__ void k_d_starts(const KT *__restrict__ keys, const unsigned *__restri
     if (blockIdx.x == 0 && threadIdx.x == 0) hstart[hcum[n]] = (unsigned)total;
 }
 
-// Writes C entry h (run h of D row d, column col).
+// Writes C entry h (run h of D row d, column col); a one-pass call writes it to the row's
+// staging slot (soff) instead.
 template <typename T>
 __device__ __forceinline__ void d_write(int h, int d, int col, typename Acc<T>::S s, const int *__restrict__ hcum,
-                                        const int *__restrict__ list, const int *__restrict__ c_rpt, int *c_col,
-                                        T *c_val, int *flags)
+                                        const int *__restrict__ list, const int *__restrict__ c_rpt,
+                                        const int *__restrict__ soff, int *c_col, T *c_val, int *flags)
 {
     const int r = __ldg(list + d);
-    const int off = __ldg(c_rpt + r);
+    const int *base = soff ? soff : c_rpt;
+    const int off = __ldg(base + r);
     const int pos = off + (h - __ldg(hcum + d));
-    if (pos < off || pos >= __ldg(c_rpt + r + 1)) {
+    if (pos < off || pos >= __ldg(base + r + 1)) {
         atomicOr(flags, kErrCountMismatch);
         return;
     }
@@ -231,9 +233,9 @@ __global__ void __launch_bounds__(kThreads) k_d_fold_short(const KT *__restrict_
                                                            const int *__restrict__ hcum, int n, int cb,
                                                            const int *__restrict__ list, const T *__restrict__ aval,
                                                            const T *__restrict__ bval, const int *__restrict__ c_rpt,
-                                                           int *__restrict__ c_col, T *__restrict__ c_val,
-                                                           unsigned *__restrict__ long_runs, int *long_count,
-                                                           int *flags)
+                                                           const int *__restrict__ soff, int *__restrict__ c_col,
+                                                           T *__restrict__ c_val, unsigned *__restrict__ long_runs,
+                                                           int *long_count, int *flags)
 {
     using AccT = Acc<T>;
     const int H = hcum[n];
@@ -261,7 +263,8 @@ __global__ void __launch_bounds__(kThreads) k_d_fold_short(const KT *__restrict_
                 if (q + u < t1) s = AccT::step(s, av[u], bv[u]);
         }
         const KT k0 = keys[t0];
-        d_write<T>(h, (int)(k0 >> cb), (int)(k0 & ((KT(1) << cb) - 1)), s, hcum, list, c_rpt, c_col, c_val, flags);
+        d_write<T>(h, (int)(k0 >> cb), (int)(k0 & ((KT(1) << cb) - 1)), s, hcum, list, c_rpt, soff, c_col, c_val,
+                   flags);
     }
 }
 
@@ -274,8 +277,8 @@ __global__ void __launch_bounds__(kThreads) k_d_fold_long(const KT *__restrict__
                                                           const int *__restrict__ hcum, int cb,
                                                           const int *__restrict__ list, const T *__restrict__ aval,
                                                           const T *__restrict__ bval, const int *__restrict__ c_rpt,
-                                                          int *__restrict__ c_col, T *__restrict__ c_val,
-                                                          const unsigned *__restrict__ long_runs,
+                                                          const int *__restrict__ soff, int *__restrict__ c_col,
+                                                          T *__restrict__ c_val, const unsigned *__restrict__ long_runs,
                                                           const int *long_count, int *flags)
 {
     using AccT = Acc<T>;
@@ -331,17 +334,40 @@ __global__ void __launch_bounds__(kThreads) k_d_fold_long(const KT *__restrict__
         }
         if (lane == 0) {
             const KT k0 = keys[t0];
-            d_write<T>(h, (int)(k0 >> cb), (int)(k0 & ((KT(1) << cb) - 1)), s, hcum, list, c_rpt, c_col, c_val,
-                       flags);
+            d_write<T>(h, (int)(k0 >> cb), (int)(k0 & ((KT(1) << cb) - 1)), s, hcum, list, c_rpt, soff, c_col,
+                       c_val, flags);
         }
         __syncwarp();
     }
 }
 
+// One-pass call: the D rows' output counts come from the head scan itself.  Row d's
+// products start at sorted position epos[dA[d]] (the sort keeps rows in order), so the
+// heads before it are hidx there; hcum[d] = those heads, c_rpt[row] = the row's heads, and
+// nnz(C) gains all of them.
+__global__ void k_d_stage_counts(const int *__restrict__ list, int n, const int *__restrict__ dA,
+                                 const int *__restrict__ epos, const unsigned *__restrict__ hidx,
+                                 const unsigned *__restrict__ flag, long long total, int *__restrict__ hcum,
+                                 int *c_rpt, unsigned long long *total_nnz)
+{
+    const int all = (int)(hidx[total - 1] + flag[total - 1]);
+    auto heads_before = [&](int d) {
+        const int p = d < n ? __ldg(epos + __ldg(dA + d)) : (int)total;
+        return p < total ? (int)hidx[p] : all;
+    };
+    for (int d = blockIdx.x * blockDim.x + threadIdx.x; d <= n; d += gridDim.x * blockDim.x) {
+        const int h0 = heads_before(d);
+        hcum[d] = h0;
+        if (d < n) c_rpt[list[d]] = heads_before(d + 1) - h0;
+        else atomicAdd(total_nnz, (unsigned long long)all);
+    }
+}
+
 template <typename T, typename KT>
 int run_d_rows_keyed(ops_handle_s *h, const SpgemmArgs<T> &g, const int *list, int n, bool numeric, cudaStream_t s,
-                     int cb, int bits)
+                     int cb, int bits, bool dry_run)
 {
+    const bool staged = numeric && g.soff != nullptr;  // one-pass call: counts found here
     const long long total = h->plan_d_flop;
     const long long ea_max = h->plan_d_len_a;  // concatenated A entries
 
@@ -365,6 +391,7 @@ int run_d_rows_keyed(ops_handle_s *h, const SpgemmArgs<T> &g, const int *list, i
     const size_t sbytes = align_up(sizeof(int) * (size_t)(n + 1), 256);
     const size_t need = 2 * kbytes + 2 * vbytes + 2 * hbytes + 2 * ebytes + 4 * sbytes + align_up(cub_bytes, 256);
     if (need > h->dense_budget) return OPS_NOT_SUPPORTED;
+    if (dry_run) return OPS_OK;
 
     void *mem = nullptr;
     OPS_CUDA(h, cudaMallocFromPoolAsync(&mem, need, h->pool, s));
@@ -402,7 +429,8 @@ int run_d_rows_keyed(ops_handle_s *h, const SpgemmArgs<T> &g, const int *list, i
     };
     size_t b = cub_bytes;
 
-    k_d_prep<<<grid_of(n + 1, kThreads, sms * 4), kThreads, 0, s>>>(list, n, g.arpt, g.c_rpt, dlen, dnnz, numeric);
+    k_d_prep<<<grid_of(n + 1, kThreads, sms * 4), kThreads, 0, s>>>(list, n, g.arpt, g.c_rpt, dlen, dnnz,
+                                                                      numeric && !staged);
     if (launched("k_d_prep")) check(cub::DeviceScan::ExclusiveSum(cub_tmp, b = cub_bytes, dlen, dA, n + 1, s), "D-row scan");
     if (st == OPS_OK) {
         k_d_elen<<<grid_of(ea_max + 1, kThreads, sms * 8), kThreads, 0, s>>>(list, n, dA, g.arpt, g.acol, g.brpt, elen);
@@ -435,7 +463,13 @@ int run_d_rows_keyed(ops_handle_s *h, const SpgemmArgs<T> &g, const int *list, i
         k_d_flags<KT><<<grid, kThreads, 0, s>>>(keys.Current(), total, flag);
         if (launched("k_d_flags"))
             check(cub::DeviceScan::ExclusiveSum(cub_tmp, b = cub_bytes, flag, hidx, (int)total, s), "head scan");
-        if (st == OPS_OK) check(cub::DeviceScan::ExclusiveSum(cub_tmp, b = cub_bytes, dnnz, hcum, n + 1, s), "row nnz scan");
+        if (st == OPS_OK && staged) {
+            k_d_stage_counts<<<grid_of(n + 1, kThreads, sms * 4), kThreads, 0, s>>>(
+                list, n, dA, epos, hidx, flag, total, hcum, g.c_rpt, &g.info->total_nnz);
+            launched("k_d_stage_counts");
+        } else if (st == OPS_OK) {
+            check(cub::DeviceScan::ExclusiveSum(cub_tmp, b = cub_bytes, dnnz, hcum, n + 1, s), "row nnz scan");
+        }
         unsigned *hstart = flag;                                                   // free after the scan
         unsigned *long_runs = reinterpret_cast<unsigned *>(vals.Alternate());    // free after the sort
         if (st == OPS_OK) {
@@ -445,14 +479,14 @@ int run_d_rows_keyed(ops_handle_s *h, const SpgemmArgs<T> &g, const int *list, i
         if (st == OPS_OK) check(cudaMemsetAsync(&g.info->d_cursor, 0, sizeof(int), s), "long-run counter");
         if (st == OPS_OK) {
             k_d_fold_short<T, KT><<<grid, kThreads, 0, s>>>(keys.Current(), vals.Current(), hstart, hcum, n, cb, list,
-                                                           g.aval, g.bval, g.c_rpt, g.c_col, g.c_val, long_runs,
-                                                           &g.info->d_cursor, &g.info->flags);
+                                                           g.aval, g.bval, g.c_rpt, g.soff, g.c_col, g.c_val,
+                                                           long_runs, &g.info->d_cursor, &g.info->flags);
             launched("k_d_fold_short");
         }
         if (st == OPS_OK) {
             k_d_fold_long<T, KT><<<sms * 8, kThreads, 0, s>>>(keys.Current(), vals.Current(), hstart, hcum, cb, list,
-                                                             g.aval, g.bval, g.c_rpt, g.c_col, g.c_val, long_runs,
-                                                             &g.info->d_cursor, &g.info->flags);
+                                                             g.aval, g.bval, g.c_rpt, g.soff, g.c_col, g.c_val,
+                                                             long_runs, &g.info->d_cursor, &g.info->flags);
             launched("k_d_fold_long");
         }
     }
@@ -465,7 +499,8 @@ int run_d_rows_keyed(ops_handle_s *h, const SpgemmArgs<T> &g, const int *list, i
 namespace opsg_internal {
 
 template <typename T>
-int run_d_rows(ops_handle_s *h, const SpgemmArgs<T> &g, const int *list, int n, bool numeric, cudaStream_t s)
+int run_d_rows(ops_handle_s *h, const SpgemmArgs<T> &g, const int *list, int n, bool numeric, cudaStream_t s,
+               bool dry_run)
 {
     const long long total = h->plan_d_flop;
     const int db = ceil_log2(std::max(n, 2));
@@ -473,11 +508,13 @@ int run_d_rows(ops_handle_s *h, const SpgemmArgs<T> &g, const int *list, int n, 
     if (total <= 0 || total > (long long)INT_MAX - 1 || h->plan_d_len_a <= 0 ||
         h->plan_d_len_a > (long long)INT_MAX - 1)
         return OPS_NOT_SUPPORTED;
-    if (db + cb <= 32) return run_d_rows_keyed<T, unsigned>(h, g, list, n, numeric, s, cb, db + cb);
-    return run_d_rows_keyed<T, unsigned long long>(h, g, list, n, numeric, s, cb, db + cb);
+    if (db + cb <= 32) return run_d_rows_keyed<T, unsigned>(h, g, list, n, numeric, s, cb, db + cb, dry_run);
+    return run_d_rows_keyed<T, unsigned long long>(h, g, list, n, numeric, s, cb, db + cb, dry_run);
 }
 
-template int run_d_rows<double>(ops_handle_s *, const SpgemmArgs<double> &, const int *, int, bool, cudaStream_t);
-template int run_d_rows<float>(ops_handle_s *, const SpgemmArgs<float> &, const int *, int, bool, cudaStream_t);
+template int run_d_rows<double>(ops_handle_s *, const SpgemmArgs<double> &, const int *, int, bool, cudaStream_t,
+                                bool);
+template int run_d_rows<float>(ops_handle_s *, const SpgemmArgs<float> &, const int *, int, bool, cudaStream_t,
+                               bool);
 
 }  // namespace opsg_internal

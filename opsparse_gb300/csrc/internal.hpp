@@ -78,6 +78,7 @@ struct ops_handle_s {
     bool staged = false;           // the counting phase of the call in progress stages
     bool stage_e1 = false;         // ... and some of its rows are E1 rows
     bool stage_e1_all = false;     // ... all of the E1 rows
+    bool stage_d = false;          // ... and the D rows (whole-GPU sort)
     unsigned char *stage = nullptr;        // [columns | values] of stage_entries entries
     size_t stage_bytes = 0;
     long long stage_entries = 0;
@@ -108,9 +109,11 @@ namespace opsg_internal {
 // D rows (more than the E2 capacity) by whole-GPU expand / stable radix sort / compress
 // (gesc.cu).  Returns OPS_NOT_SUPPORTED, having launched nothing, when the products do
 // not fit 32-bit positions or the scratch exceeds the handle's dense budget; the caller
-// then uses the dense-row kernel.
+// then uses the dense-row kernel.  numeric with g.soff set: a one-pass call, whose D rows
+// are computed into the staging area and counted into c_rpt.  dry_run: only the check.
 template <typename T>
-int run_d_rows(ops_handle_s *h, const opsg::SpgemmArgs<T> &g, const int *list, int n, bool numeric, cudaStream_t s);
+int run_d_rows(ops_handle_s *h, const opsg::SpgemmArgs<T> &g, const int *list, int n, bool numeric, cudaStream_t s,
+               bool dry_run = false);
 
 inline int status_of(cudaError_t e) { return e == cudaErrorMemoryAllocation ? OPS_OOM : OPS_CUDA_ERROR; }
 

@@ -279,11 +279,11 @@ static __global__ void __launch_bounds__(kSetupThreads) k_setup(const int *__res
         }
     }
     // products a one-pass call may compute in the counting phase (every class but R8, whose
-    // count is made here and whose numeric runs straight into C, D, and the E1
-    // column-window rows), for the prefix that places them in the staging area
+    // count is made here and whose numeric runs straight into C, and the E1 column-window
+    // rows), for the prefix that places them in the staging area
     int staged = 0;
     if (sflop) {
-        staged = (cls > kClsR8 && cls != kClsD) ? f32 : 0;
+        staged = cls > kClsR8 ? f32 : 0;
         if (cls == kClsE1 && f32 >= 16 * lenA) {
             // a column-window row keeps two passes: span of its B rows' first and last
             // columns (B rows are sorted; lenA <= 64 here)
@@ -548,6 +548,14 @@ __global__ void __launch_bounds__(256) k_reg_rows(SpgemmArgs<T> g, const int *__
         }
     }
     if (!kNum || g.soff) warp_add_u64(nnz_acc, &g.info->total_nnz);
+}
+
+// Takes a class list's rows out of a one-pass call's staging (their staged product counts
+// to zero, before the counts are scanned into offsets).
+__global__ void k_unstage_rows(const int *__restrict__ list, const int *count_ptr, int *soff)
+{
+    const int count = *count_ptr;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) soff[list[i]] = 0;
 }
 
 // Moves the staged rows of a one-pass call into C.  Row r was staged if soff[r + 1] >

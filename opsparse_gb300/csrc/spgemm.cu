@@ -170,12 +170,13 @@ int grid_for(long long work_items, int per_block, int cap)
 
 // Classes whose rows a one-pass call computes in the counting phase: all but R8 (counted
 // by k_setup; their numeric writes C directly in the second phase, next to the copy of the
-// staged rows) and D, and E1 only if some E1 row is staged (at most kE1OnePassFlopMax products, not a column-window
+// staged rows), D only if its whole-GPU sort fits the scratch budget, and E1 only if some
+// E1 row is staged (at most kE1OnePassFlopMax products, not a column-window
 // row; the split is made on the device, without such rows the E1 class keeps its own
 // list and two passes).
 bool staged_class(const ops_handle_s *h, int c)
 {
-    return c != kClsR8 && c != kClsD && (c != kClsE1 || h->stage_e1);
+    return c != kClsR8 && (c != kClsD || h->stage_d) && (c != kClsE1 || h->stage_e1);
 }
 
 // Below this many staged products the set-up of a one-pass call (the offset scan, the
@@ -311,6 +312,13 @@ int launch_staged_class(ops_handle_s *h, const GA &gs, int c, const int *list, i
             OPS_CUDA(h, cudaStreamWaitEvent(s, h->ev_x_join[1], 0));
             break;
         }
+        case kClsD: {  // whole-GPU expand/sort/compress, counts from its head scan
+            const int st_d = run_d_rows<T>(h, g, list, n, true, s);
+            if (st_d != OPS_OK) return st_d == OPS_NOT_SUPPORTED ? fail(h, OPS_CUDA_ERROR, "D-row scratch changed") : st_d;
+            h->d_rows_path[0] = n;
+            h->d_rows_path[1] = 0;
+            break;
+        }
         default:
             return fail(h, OPS_NOT_SUPPORTED, "class without a one-pass kernel");
     }
@@ -343,6 +351,22 @@ int prepare_stage(ops_handle_s *h, const DevInfo &hi, int M, cudaStream_t st)
         h->stage_bytes = total;
     }
     h->stage_entries = (long long)entries;
+    // D rows are staged only if their whole-GPU sort fits the scratch budget (else they keep
+    // two passes and the dense-row kernel may take them)
+    h->stage_d = false;
+    if (hi.counts[kClsD] > 0) {
+        SpgemmArgs<double> gd{};
+        gd.N = h->plan_N;
+        gd.soff = h->soff;
+        h->stage_d = run_d_rows<double>(h, gd, nullptr, hi.counts[kClsD], true, st, true) == OPS_OK;
+        h->last_error.clear();
+        if (!h->stage_d) {
+            k_unstage_rows<<<grid_for(hi.counts[kClsD], 256, h->num_sms * 4), 256, 0, st>>>(
+                h->lists + (size_t)kClsD * M, &h->info->counts[kClsD], h->soff);
+            OPS_CUDA(h, cudaGetLastError());
+            ++h->launches;
+        }
+    }
     size_t cb = h->cub_bytes;
     OPS_CUDA(h, cub::DeviceScan::ExclusiveSum(h->cub_tmp, cb, h->soff, h->soff, M + 1, st));
     ++h->launches;
@@ -766,8 +790,13 @@ int ops_handle_create(ops_handle_t *out)
         uint64_t thr = UINT64_MAX;
         e = cudaMemPoolSetAttribute(h->pool, cudaMemPoolAttrReleaseThreshold, &thr);
     }
+    // the D rows' whole-GPU sort is a chain of about twenty short launches, the longest
+    // path of a call that has D rows: its stream gets the highest priority, so its blocks
+    // are scheduled ahead of the other classes' waiting blocks
+    int prio_low = 0, prio_high = 0;
+    if (e == cudaSuccess) e = cudaDeviceGetStreamPriorityRange(&prio_low, &prio_high);
     for (int c = 0; c < kNumClasses && e == cudaSuccess; ++c) {
-        e = cudaStreamCreateWithFlags(&h->side[c], cudaStreamNonBlocking);
+        e = cudaStreamCreateWithPriority(&h->side[c], cudaStreamNonBlocking, c == kClsD ? prio_high : prio_low);
         if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->ev_join[c], cudaEventDisableTiming);
     }
     for (int x = 0; x < ops_handle_s::kNumExtra && e == cudaSuccess; ++x) {

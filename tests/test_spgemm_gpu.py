@@ -121,24 +121,29 @@ def test_subclass_coverage(cuda, handle):
     assert all(v > 0 for k, v in seen.items() if k != "d_dense"), seen
 
 
+@pytest.mark.parametrize("oneshot", [False, True], ids=["two_phase", "one_pass"])
 @pytest.mark.parametrize("dtype", ["f64", "f32"])
-def test_d_rows_dense_fallback(cuda, dtype):
+def test_d_rows_dense_fallback(cuda, dtype, oneshot):
     """With a scratch budget too small for the whole-GPU sort, the D rows take the
-    CTA-per-row dense kernel; both give the oracle's bits."""
+    CTA-per-row dense kernel; both give the oracle's bits.  Through ops_spgemm in one-pass
+    mode the D rows are computed while counting when the sort fits, and left to two passes
+    (the dense kernel) when it does not."""
     case = next(c for c in CASES if c[0] == "dense_row")
     name, a, b, ncols = case
     for budget, path in ((None, "d_sort"), (1 << 20, "d_dense")):
         h = ops.Handle()
+        if oneshot:
+            h.set_one_pass(2)
         if budget:
             h.set_dense_budget(budget)
         if dtype == "f64":
-            rpt, col, val = run_case(cuda, h, case, cuda.float64)
+            rpt, col, val = run_case(cuda, h, case, cuda.float64, oneshot=oneshot)
             orpt, ocol, oval = oracle.spgemm(*a, *b, ncols)
             assert np.array_equal(val.view(np.uint64), oval.view(np.uint64)), path
         else:
             a32 = (a[0], a[1], a[2].astype(np.float32))
             b32 = (b[0], b[1], b[2].astype(np.float32))
-            rpt, col, val = run_case(cuda, h, (name, a32, b32, ncols), cuda.float32)
+            rpt, col, val = run_case(cuda, h, (name, a32, b32, ncols), cuda.float32, oneshot=oneshot)
             orpt, ocol, oval = oracle.spgemm(*a32, *b32, ncols, dtype=np.float32)
             assert np.array_equal(val.view(np.uint32), oval.view(np.uint32)), path
         assert np.array_equal(rpt.astype(np.int64), orpt) and np.array_equal(col, ocol), path
@@ -219,6 +224,13 @@ def test_many_d_rows_wide(cuda, handle):
     assert np.array_equal(col, f(ocol))
     assert np.array_equal(val.view(np.uint64), oval.view(np.uint64))
     assert handle.subclass_rows()["d_sort"] > 1024
+    with ops.Handle() as h:  # the same D rows computed while counting (one pass)
+        h.set_one_pass(2)
+        rpt, col, val = run_case(cuda, h, case, cuda.float64, oneshot=True)
+        assert np.array_equal(rpt.astype(np.int64), orpt)
+        assert np.array_equal(col, f(ocol))
+        assert np.array_equal(val.view(np.uint64), oval.view(np.uint64))
+        assert h.subclass_rows()["d_sort"] > 1024
 
 
 def test_repeat_and_resize(cuda, handle):
