@@ -96,7 +96,7 @@ struct DevInfo {
     int e1_one;                   // E1 rows a one-pass call may stage
     unsigned long long d_len_a;   // A entries of the D rows
     unsigned long long d_flop;    // products of the D rows
-    int d_cursor;                 // output cursor of the D-row expansion
+    int d_cursor;                 // long runs listed by the D-row short-run fold
 };
 
 // Arguments shared by every SpGEMM kernel.

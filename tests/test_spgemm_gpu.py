@@ -287,3 +287,41 @@ def test_timings_reported(cuda, handle):
     t = handle.timings()
     assert t["total"] > 0 and t["symbolic"] > 0 and t["numeric"] > 0
     assert t["flop"] == oracle.flop(CASES[2][1][0], CASES[2][1][1], CASES[2][2][0])[0]
+
+
+def _long_run_case(seed=31):
+    """One row of 20,000 A entries over B rows that all hold the same 12 columns (plus a
+    few others): 12 output entries of 20,000 products each, far beyond a warp's batch, and
+    a D row (more than 13,312 products) for the whole-GPU sort and its long-run fold."""
+    import scipy.sparse as sp
+    from tests.cases import _csr
+    rng = np.random.default_rng(seed)
+    n = 20000
+    A = sp.csr_matrix((rng.standard_normal(n), (np.zeros(n, dtype=np.int64), np.arange(n))), shape=(2, n))
+    rows = np.repeat(np.arange(n), 12)
+    cols = np.tile(np.arange(0, 120, 10), n)
+    extra_r = rng.integers(0, n, 3000)
+    extra_c = rng.integers(0, 5000, 3000)
+    B = sp.csr_matrix((rng.standard_normal(rows.size + extra_r.size),
+                       (np.concatenate([rows, extra_r]), np.concatenate([cols, extra_c]))), shape=(n, 5000))
+    return "long_runs", _csr(A), _csr(B), 5000
+
+
+@pytest.mark.parametrize("oneshot", [False, True], ids=["two_phase", "one_pass"])
+@pytest.mark.parametrize("dtype", ["f64", "f32"])
+def test_long_runs(cuda, dtype, oneshot):
+    """Output entries folding 20,000 products each (the D rows' long-run fold): the
+    oracle's bits, two-phase and in one pass."""
+    name, a, b, ncols = _long_run_case()
+    npd = np.float64 if dtype == "f64" else np.float32
+    a = (a[0], a[1], a[2].astype(npd))
+    b = (b[0], b[1], b[2].astype(npd))
+    with ops.Handle() as h:
+        h.set_one_pass(2)
+        rpt, col, val = run_case(cuda, h, (name, a, b, ncols), getattr(cuda, "float64" if dtype == "f64" else
+                                                                       "float32"), oneshot=oneshot)
+        orpt, ocol, oval = oracle.spgemm(*a, *b, ncols, dtype=npd)
+        ut = np.uint64 if dtype == "f64" else np.uint32
+        assert np.array_equal(rpt.astype(np.int64), orpt) and np.array_equal(col, ocol)
+        assert np.array_equal(val.view(ut), oval.view(ut))
+        assert h.subclass_rows()["d_sort"] == 1
