@@ -93,12 +93,16 @@ int ops_handle_set_output_malloc(ops_handle_t handle, int use_cuda_malloc);
  * classified, computed straight into C), the rows above the E2 class, and the E1 rows
  * whose products fall within 32768 consecutive columns (banded and stencil rows, which
  * fold many products per output).  The staging area grows only and holds the eligible
- * products (column and value each), at most 2 GiB; beyond that, or if it cannot be
- * allocated, the call runs two passes.  mode 2: the same at any size.  mode 0: always two
+ * products (column and value each), at most the staging budget (2 GiB unless
+ * ops_handle_set_stage_budget says otherwise); beyond that, or if it cannot be allocated,
+ * the call runs two passes.  mode 2: the same at any size.  mode 0: always two
  * passes.  Results are identical in every mode.  ops_spgemm_symbolic and
  * ops_spgemm_numeric always run two passes.  No OpSparse counterpart: its symbolic and
  * numeric kernels always run separately (core_algo/spgemm/spgemm.cu:16-62). */
 int ops_handle_set_one_pass(ops_handle_t handle, int mode);
+/* Upper bound in bytes for the one-pass staging area (default 2 GiB); a call whose staged
+ * products need more runs two passes.  No OpSparse counterpart. */
+int ops_handle_set_stage_budget(ops_handle_t handle, size_t bytes);
 /* Row-class thresholds used by the next symbolic phase, as 6 int32 upper bounds on a
  * row's intermediate products: {R8, R16, R32, W, E1, E2} (defaults {8, 16, 32, 128, 1024,
  * 13312}, which are also the maxima; 0 switches a class off; rows above E2 use the dense

@@ -120,6 +120,10 @@ class Handle:
         """ops_spgemm in one pass: 0 off, 1 on for large inputs (default), 2 on at any size."""
         check(self.lib.ops_handle_set_one_pass(self.h, int(mode)), self.h)
 
+    def set_stage_budget(self, nbytes: int):
+        """Largest one-pass staging area; beyond it ops_spgemm runs two passes."""
+        check(self.lib.ops_handle_set_stage_budget(self.h, int(nbytes)), self.h)
+
     def set_dense_budget(self, nbytes: int):
         check(self.lib.ops_handle_set_dense_budget(self.h, int(nbytes)), self.h)
 

@@ -75,6 +75,7 @@ _SIGS = {
     "ops_handle_set_dense_budget": (C.c_int, [P, C.c_size_t]),
     "ops_handle_set_output_malloc": (C.c_int, [P, C.c_int]),
     "ops_handle_set_one_pass": (C.c_int, [P, C.c_int]),
+    "ops_handle_set_stage_budget": (C.c_int, [P, C.c_size_t]),
     "ops_handle_set_thresholds": (C.c_int, [P, C.POINTER(I32), C.c_int]),
     "ops_handle_get_thresholds": (C.c_int, [P, C.POINTER(I32), C.c_int]),
     "ops_handle_last_error": (C.c_char_p, [P]),

@@ -268,15 +268,18 @@ __global__ void __launch_bounds__(Shape::kThreads, 1) k_esc_rows(SpgemmArgs<T> g
                 unsigned key[kUnroll];
 #pragma unroll
                 for (int u = 0; u < kUnroll; ++u) key[u] = v[u] ? (unsigned)__ldg(g.bcol + kk[u]) : 0u;
+                bool bad = false;
 #pragma unroll
                 for (int u = 0; u < kUnroll; ++u) {
                     const int i = c0 + u * NT + lane;
                     if (v[u]) {
+                        bad |= key[u] >= (unsigned)g.N;
                         key0[i] = key[u];
                         id0[i] = (unsigned short)i;
                         own[i] = (unsigned short)oo[u];
                     }
                 }
+                if (bad) atomicOr(&g.info->flags, kErrBadColumn);  // B column outside [0, N)
             }
             __syncthreads();
             unsigned *kin = key0, *kout = key1;

@@ -509,6 +509,8 @@ __global__ void __launch_bounds__(256) k_reg_rows(SpgemmArgs<T> g, const int *__
         const int o_b0 = __shfl_sync(kFull, b0, lo, G);
         const int k = o_b0 + (q - (o_incl - o_bl));
         const int col = valid ? __ldg(g.bcol + k) : kEmpty;
+        if (__any_sync(kFull, valid && (unsigned)col >= (unsigned)g.N) && lane == 0)
+            atomicOr(&g.info->flags, kErrBadColumn);  // B column outside [0, N)
         const unsigned m = __match_any_sync(kFull, col) & gmask;
         const bool leader = valid && (lane == __ffs(m) - 1);
 

@@ -904,6 +904,13 @@ int ops_handle_set_one_pass(ops_handle_t h, int mode)
     return OPS_OK;
 }
 
+int ops_handle_set_stage_budget(ops_handle_t h, size_t bytes)
+{
+    if (!h) return OPS_INVALID_ARGUMENT;
+    h->stage_budget = bytes;
+    return OPS_OK;
+}
+
 int ops_handle_set_output_malloc(ops_handle_t h, int use_cuda_malloc)
 {
     if (!h) return OPS_INVALID_ARGUMENT;

@@ -244,6 +244,29 @@ def test_repeat_and_resize(cuda, handle):
         assert np.array_equal(x, y)
 
 
+@pytest.mark.parametrize("budget", [None, 1 << 16], ids=["staged", "over_budget"])
+def test_one_pass_resize_and_budget(cuda, budget):
+    """One-pass calls on one handle across sizes and value types (the staging area grows
+    and is reused), and with a staging budget too small for the inputs (two passes
+    instead): the oracle's bits every time."""
+    with ops.Handle() as h:
+        h.set_one_pass(2)
+        if budget:
+            h.set_stage_budget(budget)
+        for case, dtype in ((CASES[0], "f64"), (CASES[2], "f64"), (CASES[4], "f32"), (CASES[0], "f32"),
+                            (CASES[2], "f64")):
+            name, a, b, ncols = case
+            npd = np.float64 if dtype == "f64" else np.float32
+            a = (a[0], a[1], a[2].astype(npd))
+            b = (b[0], b[1], b[2].astype(npd))
+            rpt, col, val = run_case(cuda, h, (name, a, b, ncols),
+                                     cuda.float64 if dtype == "f64" else cuda.float32, oneshot=True)
+            orpt, ocol, oval = oracle.spgemm(*a, *b, ncols, dtype=npd)
+            ut = np.uint64 if dtype == "f64" else np.uint32
+            assert np.array_equal(rpt.astype(np.int64), orpt) and np.array_equal(col, ocol), name
+            assert np.array_equal(val.view(ut), oval.view(ut)), name
+
+
 def test_empty_inputs(cuda, handle):
     z = (np.zeros(1, np.int32), np.zeros(0, np.int32), np.zeros(0))
     C = handle.spgemm(ops.csr_to_device(*z, 0, 0), ops.csr_to_device(*z, 0, 0))
@@ -262,6 +285,22 @@ def test_invalid_column_is_reported(cuda, handle):
     with pytest.raises(ops.OpsError) as ei:
         handle.symbolic(A, A)
     assert ei.value.status == ops.capi.OPS_INVALID_CSR
+
+
+@pytest.mark.parametrize("one_pass", [2, 0], ids=["one_pass", "two_pass"])
+def test_invalid_b_column_is_reported(cuda, one_pass):
+    """A column of B outside [0, cols) under a row of 9-16 products (the R16 class) is
+    reported by ops_spgemm as invalid CSR, whether the row is computed while counting or
+    in two passes."""
+    A = ops.csr_to_device(np.array([0, 3], np.int32), np.array([0, 1, 2], np.int32), np.ones(3), 1, 3)
+    brpt = np.array([0, 4, 8, 12], np.int32)
+    bcol = np.array([0, 1, 2, 3, 0, 1, 2, 9, 0, 1, 2, 3], np.int32)  # 9 >= cols (4)
+    B = ops.csr_to_device(brpt, bcol, np.ones(12), 3, 4)
+    with ops.Handle() as h:
+        h.set_one_pass(one_pass)
+        with pytest.raises(ops.OpsError) as ei:
+            h.spgemm_oneshot(A, B)
+        assert ei.value.status == ops.capi.OPS_INVALID_CSR
 
 
 def test_numeric_without_symbolic_is_rejected(cuda):
