@@ -171,38 +171,28 @@ __device__ __forceinline__ int besc_sort_fold(const SpgemmArgs<T> &g, int n, int
         if (tid == 0) hidx[total] = n;
         __syncthreads();
         if (tid == 0 && !g.soff && total != n_expect) atomicOr(&g.info->flags, kErrCountMismatch);
-        // runs in head order: consecutive threads write consecutive entries of C.  A run
-        // is folded kUnroll products at a time, their operands loaded together.
-        for (int hh = tid; hh < total; hh += NT) {
-            const int e0 = hidx[hh], e1 = hidx[hh + 1];
-            S s = AccT::zero();
-            int col = 0;
-            for (int t = e0; t < e1; t += kUnroll) {
-                T av[kUnroll], bv[kUnroll];
-                int kk0 = 0;
-#pragma unroll
-                for (int u = 0; u < kUnroll; ++u) {
-                    av[u] = T(0);
-                    bv[u] = T(0);
-                    if (t + u < e1) {
-                        const int q = spid[t + u];
-                        const int o = own[q];
-                        const int k = s_b0[o] + q - (o ? s_incl[o - 1] : 0);
-                        if (u == 0) kk0 = k;
-                        av[u] = __ldg(g.aval + a0 + o);
-                        bv[u] = __ldg(g.bval + k);
-                    }
+        // runs in head order (thread tid takes runs tid, tid + NT, ...: consecutive threads
+        // write consecutive entries of C), each thread walking its runs one product per
+        // step with the operands of kFoldUnroll steps loaded together: a warp issues about
+        // as many FP64 FMAs as its busiest lane has products, where a fixed kUnroll-wide
+        // fold per run issued kUnroll FMAs for a run of one product
+        const int K = tid < total ? (total - tid + NT - 1) / NT : 0;
+        fold_own_runs<T>(
+            0, K, INT_MAX, [&](int k) { return hidx[tid + k * NT]; }, [&](int k) { return hidx[tid + k * NT + 1]; },
+            [&](int t, T &a, T &b, int &kb) {
+                const int q = spid[t];
+                const int o = own[q];
+                kb = s_b0[o] + q - (o ? s_incl[o - 1] : 0);
+                a = __ldg(g.aval + a0 + o);
+                b = __ldg(g.bval + kb);
+            },
+            [&](int k, int, int kb, S s) {
+                const int hh = tid + k * NT;
+                if (hh < n_expect) {
+                    g.c_col[off + hh] = __ldg(g.bcol + kb);
+                    g.c_val[off + hh] = AccT::fin(s);
                 }
-                if (t == e0) col = __ldg(g.bcol + kk0);
-#pragma unroll
-                for (int u = 0; u < kUnroll; ++u)
-                    if (t + u < e1) s = AccT::step(s, av[u], bv[u]);
-            }
-            if (hh < n_expect) {
-                g.c_col[off + hh] = col;
-                g.c_val[off + hh] = AccT::fin(s);
-            }
-        }
+            });
     }
     return total;
 }
