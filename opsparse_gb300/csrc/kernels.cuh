@@ -16,6 +16,10 @@
 //   k_dense_rows       <- the global-hash fallback (symbolic.cuh:263-325, numeric.cuh:304-393):
 //                         one CTA per row over a dense accumulator and bitmap in HBM, which
 //                         also yields ascending columns without a sort.
+//   k_small_rows       <- k_numeric_shared_hash_pwarp for rows of at most 8 products: one
+//                         thread per row, a sorting network in registers.
+//   k_place_staged     no counterpart: copies the rows a one-pass call computed while
+//                         counting from the staging area into C.
 //
 // Numeric values are folded in ascending j for every output entry (see common.cuh), so
 // all classes produce the same bits as the CPU oracle.
