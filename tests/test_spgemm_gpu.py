@@ -278,6 +278,42 @@ def test_empty_inputs(cuda, handle):
     assert C.nnz == 0 and np.all(C.rpt.cpu().numpy() == 0)
 
 
+@pytest.mark.parametrize("case", [CASES[2], CASES[4], CASES[6]], ids=[IDS[2], IDS[4], IDS[6]])
+def test_numeric_after_one_pass_call(cuda, case):
+    """The plan an ops_spgemm call leaves on the handle (its counting phase computed most
+    rows in one pass) serves ops_spgemm_numeric with new values: every class's two-pass
+    numeric runs on the lists that call made, and gives the oracle's bits."""
+    name, a, b, ncols = case
+    kcols = len(b[0]) - 1
+    with ops.Handle() as h:
+        h.set_one_pass(2)
+        A = to_dev(cuda, a, kcols, cuda.float64)
+        B = to_dev(cuda, b, ncols, cuda.float64)
+        C = h.spgemm_oneshot(A, B)
+        a2 = (a[0], a[1], a[2] * 1.5 - 0.25)
+        A2 = to_dev(cuda, a2, kcols, cuda.float64)
+        A2 = ops.CsrMatrix(A.rows, A.cols, A.rpt, A.col, A2.val)  # same structure arrays as the plan
+        c_col, c_val = h.numeric(A2, B, C.rpt, C.nnz)
+        cuda.cuda.synchronize()
+        orpt, ocol, oval = oracle.spgemm(*a2, *b, ncols)
+        assert np.array_equal(C.rpt.cpu().numpy().astype(np.int64), orpt)
+        assert np.array_equal(c_col.cpu().numpy(), ocol)
+        assert np.array_equal(c_val.cpu().numpy().view(np.uint64), oval.view(np.uint64))
+
+
+def test_empty_inputs_one_pass(cuda):
+    """ops_spgemm on empty and structurally empty inputs with one pass forced on."""
+    with ops.Handle() as h:
+        h.set_one_pass(2)
+        z = (np.zeros(1, np.int32), np.zeros(0, np.int32), np.zeros(0))
+        C = h.spgemm_oneshot(ops.csr_to_device(*z, 0, 0), ops.csr_to_device(*z, 0, 0))
+        assert C.nnz == 0 and C.rpt.numel() == 1
+        A = ops.csr_to_device(np.zeros(6, np.int32), np.zeros(0, np.int32), np.zeros(0), 5, 7)
+        B = ops.csr_to_device(np.zeros(8, np.int32), np.zeros(0, np.int32), np.zeros(0), 7, 9)
+        C = h.spgemm_oneshot(A, B)
+        assert C.nnz == 0 and np.all(C.rpt.cpu().numpy() == 0)
+
+
 def test_invalid_column_is_reported(cuda, handle):
     rpt = np.array([0, 2, 3], np.int32)
     col = np.array([0, 5, 1], np.int32)  # 5 >= cols (3)
