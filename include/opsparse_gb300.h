@@ -86,13 +86,13 @@ int ops_handle_set_dense_budget(ops_handle_t handle, size_t bytes);
  * expects). */
 int ops_handle_set_output_malloc(ops_handle_t handle, int use_cuda_malloc);
 /* One pass in ops_spgemm, where the values are known before the counting phase.  mode 1
- * (default): when at least 2^20 products are eligible, the rows of the R16 to E2 classes
+ * (default): when at least 2^20 products are eligible, the rows of the R16 to D classes
  * (see ops_handle_set_thresholds) are computed during the counting phase into a staging
  * area held by the handle and copied into C after the row_ptr scan, instead of reading A
  * and B again in a second pass.  Left to two passes: the R8 rows (counted while they are
- * classified, computed straight into C), the rows above the E2 class, and the E1 rows
- * whose products fall within 32768 consecutive columns (banded and stencil rows, which
- * fold many products per output).  The staging area grows only and holds the eligible
+ * classified, computed straight into C), the E1 rows whose products fall within 32768
+ * consecutive columns (banded and stencil rows, which fold many products per output), and
+ * the D rows when their whole-GPU sort would exceed the dense-row budget.  The staging area grows only and holds the eligible
  * products (column and value each), at most the staging budget (2 GiB unless
  * ops_handle_set_stage_budget says otherwise); beyond that, or if it cannot be allocated,
  * the call runs two passes.  mode 2: the same at any size.  mode 0: always two

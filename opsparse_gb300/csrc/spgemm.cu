@@ -171,9 +171,8 @@ int grid_for(long long work_items, int per_block, int cap)
 // Classes whose rows a one-pass call computes in the counting phase: all but R8 (counted
 // by k_setup; their numeric writes C directly in the second phase, next to the copy of the
 // staged rows), D only if its whole-GPU sort fits the scratch budget, and E1 only if some
-// E1 row is staged (at most kE1OnePassFlopMax products, not a column-window
-// row; the split is made on the device, without such rows the E1 class keeps its own
-// list and two passes).
+// E1 row is staged (not a column-window row; the split is made on the device, and without
+// such rows the E1 class keeps its own list and two passes).
 bool staged_class(const ops_handle_s *h, int c)
 {
     return c != kClsR8 && (c != kClsD || h->stage_d) && (c != kClsE1 || h->stage_e1);
