@@ -146,6 +146,18 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(rows)}
 
 
+def max_over_ranks(value: float, world: int, device) -> float:
+    """The largest of every rank's `value` (the slowest rank's time); `value` itself when
+    there is one rank."""
+    if world <= 1:
+        return float(value)
+    import torch
+
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
 # ----------------------------------------------------------------------------- CPU side
 def _pair(data):
     """Plain workloads are C = A*A (one CSR triple) or C = A*B (a pair of triples)."""
@@ -330,11 +342,7 @@ def run_ours(args, desc, dt, data, n, rank, world, local_rank):
     if world > 1:
         torch.distributed.barrier()
     step_ms = [a.elapsed_time(b) for a, b in ev]
-    t_ms = float(np.mean(step_ms))
-    if world > 1:
-        tt = torch.tensor([t_ms], dtype=torch.float64, device=dev)
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        t_ms = float(tt.item())
+    t_ms = max_over_ranks(float(np.mean(step_ms)), world, dev)
     gflops = world * 2.0 * P / (t_ms * 1e-3) / 1e9
 
     # end to end through the same call with host buffers
@@ -391,11 +399,7 @@ def run_ours(args, desc, dt, data, n, rank, world, local_rank):
         release((rp2, cp2, vp2))
         if i >= args.warmup:
             e2e_ms.append(e0.elapsed_time(e1))
-    e2e_t = float(np.mean(e2e_ms))
-    if world > 1:
-        tt = torch.tensor([e2e_t], dtype=torch.float64, device=dev)
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        e2e_t = float(tt.item())
+    e2e_t = max_over_ranks(float(np.mean(e2e_ms)), world, dev)
     e2e_gf = world * 2.0 * P / (e2e_t * 1e-3) / 1e9
 
     if rank != 0:
@@ -505,12 +509,12 @@ def run_batched(args, rank, world, local_rank):
     import opsparse_gb300 as ops
     from opsparse_gb300 import capi, gen_device
 
-    torch.cuda.set_device(local_rank)
-    if args.impl == "reference":
+    if args.impl == "reference":  # answered without touching a GPU
         if rank == 0:
             print(json.dumps({"metric": METRIC, "impl": "reference", "unavailable":
                               "OpSparse has no batched SpGEMM and no CPU SpGEMM; see the plain workloads"}))
         return
+    torch.cuda.set_device(local_rank)
     sizes, row_base, a_side, b_side = gen_device.er_batch(args.batch, dtype=torch.float32)
     A = gen_device.problem_slices(sizes, row_base, a_side)
     B = gen_device.problem_slices(sizes, row_base, b_side)
@@ -586,12 +590,12 @@ def run_backward(args, rank, world, local_rank):
     from opsparse_gb300 import gen
     from opsparse_gb300.autograd import FixedPatternSpGEMM
 
-    torch.cuda.set_device(local_rank)
-    if args.impl == "reference":
+    if args.impl == "reference":  # answered without touching a GPU
         if rank == 0:
             print(json.dumps({"metric": METRIC, "impl": "reference", "unavailable":
                               "OpSparse has no backward pass; see the plain workloads"}))
         return
+    torch.cuda.set_device(local_rank)
     dt = torch.float32 if args.workload.endswith("f32") else torch.float64
     n = 200_000
     a = gen.powerlaw_square(n, 16, 2.2)
