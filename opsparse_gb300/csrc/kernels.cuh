@@ -746,17 +746,29 @@ __device__ __forceinline__ void row_window(const SpgemmArgs<T> &g, int a0, int a
 // Sets the bits of the row's columns (offsets from cmin, at most span).  Returns true on
 // every lane if a column fell outside [cmin, cmin + span] (a B row out of order).
 template <typename T>
+// Counting needs no order, so each lane walks whole B rows of its own (one per A entry,
+// four columns' loads in flight), with no per-row broadcast of the B row's extent.
 __device__ __forceinline__ bool window_mark(const SpgemmArgs<T> &g, int a0, int a1, int cmin, int span,
                                             unsigned *bits)
 {
+    const int lane = lane_id();
     bool bad = false;
-    warp_rowwise_products_pf<4, false, T>(a0, a1, g.acol, g.aval, g.brpt, g.bcol, g.bval, [&](bool valid, int col, T, T) {
-        if (valid) {
-            const int o = col - cmin;
-            if ((unsigned)o <= (unsigned)span) atomicOr(bits + (o >> 5), 1u << (o & 31));
-            else bad = true;
+    for (int q = a0 + lane; q < a1; q += 32) {
+        const int j = __ldg(g.acol + q);
+        const int b1 = __ldg(g.brpt + j + 1);
+        for (int p = __ldg(g.brpt + j); p < b1; p += 4) {
+            int col[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) col[u] = p + u < b1 ? __ldg(g.bcol + p + u) : 0;
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                if (p + u >= b1) break;
+                const int o = col[u] - cmin;
+                if ((unsigned)o <= (unsigned)span) atomicOr(bits + (o >> 5), 1u << (o & 31));
+                else bad = true;
+            }
         }
-    });
+    }
     __syncwarp();
     return __any_sync(kFull, bad);
 }
