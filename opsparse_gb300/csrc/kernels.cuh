@@ -773,25 +773,125 @@ __device__ __forceinline__ bool window_mark(const SpgemmArgs<T> &g, int a0, int 
     return __any_sync(kFull, bad);
 }
 
+// Counts the set bits of bitmap words [0, nw) and clears them, four words (one 16-byte
+// shared access) per lane step.  Words past nw up to the next multiple of four are zero
+// (never marked), and nw <= kWinWords, a multiple of four.  Returns the count on every lane.
+__device__ __forceinline__ int window_sweep(unsigned *bits, int nw)
+{
+    uint4 *b4 = reinterpret_cast<uint4 *>(bits);
+    int cnt = 0;
+    for (int w = lane_id(); w < (nw + 3) >> 2; w += 32) {
+        const uint4 x = b4[w];
+        cnt += __popc(x.x) + __popc(x.y) + __popc(x.z) + __popc(x.w);
+        b4[w] = make_uint4(0u, 0u, 0u, 0u);
+    }
+    return (int)__reduce_add_sync(kFull, (unsigned)cnt);
+}
+
+__device__ __forceinline__ void window_store_count(int *c_rpt, int r, int total, unsigned long long &nnz_acc)
+{
+    if (lane_id() == 0) {
+        c_rpt[r] = total;
+        nnz_acc += (unsigned long long)total;
+    }
+    __syncwarp();
+}
+
 // Distinct-column count of one window row, written to c_rpt[r].  All lanes call it.
 template <typename T>
 __device__ __forceinline__ void window_count_row(const SpgemmArgs<T> &g, int r, int a0, int a1, int cmin, int cmax,
                                                  unsigned *bits, unsigned long long &nnz_acc)
 {
-    const int lane = lane_id();
-    if (window_mark<T>(g, a0, a1, cmin, cmax - cmin, bits) && lane == 0) atomicOr(&g.info->flags, kErrBadColumn);
-    const int nw = ((cmax - cmin) >> 5) + 1;
-    int cnt = 0;
-    for (int w = lane; w < nw; w += 32) {
-        cnt += __popc(bits[w]);
-        bits[w] = 0u;
+    const bool bad = window_mark<T>(g, a0, a1, cmin, cmax - cmin, bits) || cmin < 0 || cmax >= g.N;
+    if (bad && lane_id() == 0) atomicOr(&g.info->flags, kErrBadColumn);
+    window_store_count(g.c_rpt, r, window_sweep(bits, ((cmax - cmin) >> 5) + 1), nnz_acc);
+}
+
+// B-row quads (16-byte loads) a lane has in flight in the short-row window count.
+constexpr int kWinQuads = 8;
+
+// Marks the columns of one batch of a lane's B row: quads v[u] hold columns q0 + 4u .. +3;
+// those below b0 (first quad only, lo = b0 - q0) or from b1 on are not the row's.
+__device__ __forceinline__ void window_mark_quads(const int4 (&v)[kWinQuads], int q0, int lo, int b1, int cmin,
+                                                  unsigned span, unsigned *bits, bool &bad)
+{
+#pragma unroll
+    for (int u = 0; u < kWinQuads; ++u) {
+        const int e[4] = {v[u].x, v[u].y, v[u].z, v[u].w};
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            if ((u != 0 || k >= lo) && q0 + 4 * u + k < b1) {
+                const unsigned o = (unsigned)(e[k] - cmin);
+                if (o <= span) atomicOr(bits + (o >> 5), 1u << (o & 31));
+                else bad = true;
+            }
+        }
     }
-    const int total = (int)__reduce_add_sync(kFull, (unsigned)cnt);
-    if (lane == 0) {
-        g.c_rpt[r] = total;
-        nnz_acc += (unsigned long long)total;
+}
+
+// Loads one batch of a lane's B row: the quads at q0, q0 + 4, ... that start before b1.
+// vec: 16-byte loads (B's column array is 16-byte aligned and the lane's last quad ends
+// inside it); otherwise the row's columns one by one.
+__device__ __forceinline__ void window_load_quads(const int *__restrict__ bcol, int q0, int b0, int b1, bool vec,
+                                                  int4 (&v)[kWinQuads])
+{
+#pragma unroll
+    for (int u = 0; u < kWinQuads; ++u) {
+        const int q = q0 + 4 * u;
+        if (q < b1) {
+            if (vec) {
+                v[u] = __ldg(reinterpret_cast<const int4 *>(bcol + q));
+            } else {
+                v[u].x = q >= b0 ? __ldg(bcol + q) : 0;
+                v[u].y = q + 1 >= b0 && q + 1 < b1 ? __ldg(bcol + q + 1) : 0;
+                v[u].z = q + 2 >= b0 && q + 2 < b1 ? __ldg(bcol + q + 2) : 0;
+                v[u].w = q + 3 < b1 ? __ldg(bcol + q + 3) : 0;
+            }
+        }
+    }
+}
+
+// Column-window count of a row with at most 32 A entries, a lane per A entry.  The lane's
+// B row is read as 16-byte quads, up to kWinQuads in flight, issued together with the
+// loads of its first and last column that give the window: a stencil row takes three
+// dependent round trips to L2 (A's column, B's row extent, B's columns) where reading the
+// window first and the rows after takes five.  Returns false, having marked nothing, when
+// the products do not fit a window of kWinBits columns.
+template <typename T>
+__device__ __forceinline__ bool window_row_short(const SpgemmArgs<T> &g, int r, int a0, int a1, int nnz_b,
+                                                 bool bcol16, unsigned *bits, bool &clean,
+                                                 unsigned long long &nnz_acc)
+{
+    const int lane = lane_id();
+    int b0 = 0, b1 = 0;
+    if (a0 + lane < a1) {
+        const int j = __ldg(g.acol + a0 + lane);
+        b0 = __ldg(g.brpt + j);
+        b1 = __ldg(g.brpt + j + 1);
+    }
+    const int q0 = b0 & ~3;
+    const bool vec = bcol16 && ((b1 + 3) & ~3) <= nnz_b;
+    int4 v[kWinQuads];
+    window_load_quads(g.bcol, q0, b0, b1, vec, v);
+    const int cmin = __reduce_min_sync(kFull, b1 > b0 ? __ldg(g.bcol + b0) : INT_MAX);
+    const int cmax = __reduce_max_sync(kFull, b1 > b0 ? __ldg(g.bcol + b1 - 1) : -1);
+    if (!(cmax >= cmin && cmax - cmin < kWinBits)) return false;
+    if (!clean) {
+        for (int i = lane; i < kWinWords; i += 32) bits[i] = 0u;
+        __syncwarp();
+        clean = true;
+    }
+    const unsigned span = (unsigned)(cmax - cmin);
+    bool bad = cmin < 0 || cmax >= g.N;
+    window_mark_quads(v, q0, b0 - q0, b1, cmin, span, bits, bad);
+    for (int q = q0 + 4 * kWinQuads; q < b1; q += 4 * kWinQuads) {
+        window_load_quads(g.bcol, q, b0, b1, vec, v);
+        window_mark_quads(v, q, 0, b1, cmin, span, bits, bad);
     }
     __syncwarp();
+    if (__any_sync(kFull, bad) && lane == 0) atomicOr(&g.info->flags, kErrBadColumn);
+    window_store_count(g.c_rpt, r, window_sweep(bits, (int)(span >> 5) + 1), nnz_acc);
+    return true;
 }
 
 template <bool kNum, typename T, int TMAX>
@@ -812,9 +912,17 @@ __global__ void __launch_bounds__(kWarpRowsThreads) k_warp_rows(SpgemmArgs<T> g,
     const long long warp0 = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
     unsigned long long nnz_acc = 0;
+    int nnz_b = 0;
+    bool bcol16 = false;
+    if constexpr (!kNum) {
+        nnz_b = __ldg(g.brpt + g.K);
+        bcol16 = ((size_t)g.bcol & 15) == 0;
+    }
 
-    for (long long it = warp0; it < count; it += nwarps) {
-        const int r = __ldg(list + it);
+    // the next row's number is loaded a row ahead
+    int r = warp0 < count ? __ldg(list + warp0) : 0, r_next = 0;
+    for (long long it = warp0; it < count; it += nwarps, r = r_next) {
+        r_next = it + nwarps < count ? __ldg(list + it + nwarps) : 0;
         const int a0 = __ldg(g.arpt + r);
         const int a1 = __ldg(g.arpt + r + 1);
         int n_expect = 0, off = 0;
@@ -830,8 +938,10 @@ __global__ void __launch_bounds__(kWarpRowsThreads) k_warp_rows(SpgemmArgs<T> g,
                                 : max(5, ceil_log2(2 * max(n_expect, 1)));
         const int row_products = kNum ? __ldg(g.row_flop + r) : n_expect;
         const bool rowwise = row_products >= 16 * (a1 - a0);
-        if (!kNum && rowwise) {
+        if (!kNum && rowwise && a1 - a0 <= 32) {
             // long B rows: do all the products fit a window of kWinBits columns?
+            if (window_row_short<T>(g, r, a0, a1, nnz_b, bcol16, wbits, win_clean, nnz_acc)) continue;
+        } else if (!kNum && rowwise) {
             int cmin, cmax;
             row_window<T>(g, a0, a1, cmin, cmax);
             if (cmax >= cmin && cmax - cmin < kWinBits) {

@@ -400,3 +400,64 @@ def test_long_runs(cuda, dtype, oneshot):
         assert np.array_equal(rpt.astype(np.int64), orpt) and np.array_equal(col, ocol)
         assert np.array_equal(val.view(ut), oval.view(ut))
         assert h.subclass_rows()["d_sort"] == 1
+
+
+def _banded(n, half, seed):
+    """n x n banded CSR: row r holds columns r - half .. r + half within [0, n)."""
+    rng = np.random.default_rng(seed)
+    lens = np.array([min(n, r + half + 1) - max(0, r - half) for r in range(n)])
+    rpt = np.zeros(n + 1, np.int32)
+    rpt[1:] = np.cumsum(lens)
+    col = np.concatenate([np.arange(max(0, r - half), min(n, r + half + 1)) for r in range(n)]).astype(np.int32)
+    return rpt, col, rng.uniform(-1.0, 1.0, col.size)
+
+
+def _window_operands(cuda, shape, n=3001):
+    a = _banded(n, 13 if shape == "short" else 19, 11)  # 27 or 39 A entries per row
+    b = _banded(n, 12, 12)  # B rows of 25 columns: 675 or 975 products, E1 rows read row-wise
+    return a, b
+
+
+@pytest.mark.parametrize("shape", ["short", "long"])
+@pytest.mark.parametrize("misaligned", [False, True], ids=["bcol16", "bcol_offset4"])
+@pytest.mark.parametrize("one_pass", [2, 0], ids=["one_pass", "two_pass"])
+def test_window_rows(cuda, shape, misaligned, one_pass):
+    """Banded A·B: E1 rows with long B rows whose products fall in a window of columns are
+    counted over a bitmap.  With at most 32 A entries ("short") a lane per entry reads its
+    B row as 16-byte quads, or column by column where B's column array is not 16-byte
+    aligned and for the last B rows (nnz(B) is not a multiple of 4); with more ("long") the
+    window is read first.  The oracle's bits, two-phase and in one pass."""
+    n = 3001
+    a, b = _window_operands(cuda, shape, n)
+    assert b[1].size % 4 != 0
+    A = ops.csr_to_device(*a, n, n, dtype=cuda.float64)
+    B = ops.csr_to_device(*b, n, n, dtype=cuda.float64)
+    if misaligned:
+        buf = cuda.zeros(b[1].size + 1, dtype=cuda.int32, device=B.col.device)
+        buf[1:] = B.col
+        B = ops.CsrMatrix(B.rows, B.cols, B.rpt, buf[1:], B.val)
+        assert B.col.data_ptr() % 16 != 0
+    orpt, ocol, oval = oracle.spgemm(*a, *b, n)
+    with ops.Handle() as h:
+        h.set_one_pass(one_pass)
+        rpt, col, val = h.spgemm_oneshot(A, B).to_host()
+    assert np.array_equal(rpt.astype(np.int64), orpt) and np.array_equal(col, ocol)
+    assert np.array_equal(val.view(np.uint64), oval.view(np.uint64))
+
+
+@pytest.mark.parametrize("shape", ["short", "long"])
+@pytest.mark.parametrize("one_pass", [2, 0], ids=["one_pass", "two_pass"])
+def test_invalid_b_column_in_window_row(cuda, shape, one_pass):
+    """A column of B at or past cols as the last (largest) column of a B row that window
+    rows read: reported as invalid CSR by the counting of those rows."""
+    n = 400
+    a, b = _window_operands(cuda, shape, n)
+    bcol = b[1].copy()
+    bcol[b[0][201] - 1] = n + 7  # B row 200 stays sorted
+    A = ops.csr_to_device(*a, n, n, dtype=cuda.float64)
+    B = ops.csr_to_device(b[0], bcol, b[2], n, n, dtype=cuda.float64)
+    with ops.Handle() as h:
+        h.set_one_pass(one_pass)
+        with pytest.raises(ops.OpsError) as ei:
+            h.spgemm_oneshot(A, B)
+        assert ei.value.status == ops.capi.OPS_INVALID_CSR
