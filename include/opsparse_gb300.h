@@ -202,6 +202,9 @@ int ops_batch_check(ops_batch_t batch, void *stream);
 int ops_batch_result(ops_batch_t batch, int32_t index, int32_t **c_rpt, int32_t **c_col, void **c_val,
                      int64_t *c_nnz);
 int ops_batch_info(ops_batch_t batch, int32_t *segments, int64_t *flop, int64_t *nnz);
+/* Releases the batch (synchronizes).  Its device memory returns to the handle's pool and
+ * its per-segment handles to the handle, both reused by the handle's next batch; destroy
+ * every batch before its handle. */
 int ops_batch_destroy(ops_batch_t batch);
 
 /* ----------------------------------------------------------------- autotuner -- */

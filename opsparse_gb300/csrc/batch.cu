@@ -190,7 +190,7 @@ struct ops_batch_s {
     Item *d_items = nullptr;
     std::vector<Segment> segs;
     int *c_rpt_arena = nullptr;  // all rebased per-problem row pointers
-    void *mem = nullptr;         // one pool allocation for inputs and outputs of all segments
+    void *mem = nullptr;         // one allocation for every segment's inputs and row pointers
     long long flop = 0, nnz = 0;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
@@ -205,6 +205,11 @@ extern "C" int ops_spgemm_numeric(ops_handle_t, int, int32_t, int32_t, int32_t, 
 
 namespace {
 
+// A batch's device memory comes from its handle's stream-ordered pool, which keeps freed
+// memory for the next allocation: a repeated batch of similar size (and the autotuner's
+// candidate runs) maps no new memory for its outputs (tens of GB for thousands of
+// problems) and creates no new segment handles.  The memory goes back to the pool here,
+// after the device is idle, and the segment handles go to the handle's spares.
 void batch_release(ops_batch_s *b)
 {
     if (!b) return;
@@ -212,12 +217,13 @@ void batch_release(ops_batch_s *b)
     if (b->exec) cudaGraphExecDestroy(b->exec);
     if (b->graph) cudaGraphDestroy(b->graph);
     for (Segment &s : b->segs) {
-        if (s.h) ops_handle_destroy(s.h);
-        if (s.c_col) cudaFree(s.c_col);
-        if (s.c_val) cudaFree(s.c_val);
+        if (s.h) b->owner->spare.push_back(s.h);
+        if (s.c_col) cudaFreeAsync(s.c_col, 0);
+        if (s.c_val) cudaFreeAsync(s.c_val, 0);
     }
-    if (b->mem) cudaFree(b->mem);
-    if (b->d_items) cudaFree(b->d_items);
+    if (b->mem) cudaFreeAsync(b->mem, 0);
+    if (b->d_items) cudaFreeAsync(b->d_items, 0);
+    cudaStreamSynchronize(0);
     (void)cudaGetLastError();
     delete b;
 }
@@ -280,7 +286,7 @@ extern "C" int ops_batch_create(ops_handle_t h, int dtype, int32_t count, const 
     }
     {
         void *p = nullptr;
-        cudaError_t e = cudaMalloc(&p, sizeof(Item) * std::max(count, 1));
+        cudaError_t e = cudaMallocFromPoolAsync(&p, sizeof(Item) * std::max(count, 1), h->pool, st);
         if (e != cudaSuccess) return bail(fail(h, status_of(e), "allocating batch descriptors"));
         b->d_items = static_cast<Item *>(p);
         void *f = nullptr;
@@ -349,7 +355,7 @@ extern "C" int ops_batch_create(ops_handle_t h, int dtype, int32_t count, const 
     size_t total = align_up(4 * (size_t)std::max(1LL, rb), 256);
     for (const Segment &s : b->segs) total += seg_bytes(s, vs);
     {
-        cudaError_t e = cudaMalloc(&b->mem, total);
+        cudaError_t e = cudaMallocFromPoolAsync(&b->mem, total, h->pool, st);
         if (e != cudaSuccess) return bail(fail(h, status_of(e), "allocating batch arena"));
         e = cudaMemcpyAsync(b->d_items, b->items.data(), sizeof(Item) * count, cudaMemcpyHostToDevice, st);
         if (e != cudaSuccess) return bail(fail(h, status_of(e), "copying batch descriptors"));
@@ -389,7 +395,13 @@ extern "C" int ops_batch_create(ops_handle_t h, int dtype, int32_t count, const 
         }
         if (e == cudaSuccess) e = cudaStreamSynchronize(st);  // host values above must outlive the copies
         if (e != cudaSuccess) return bail(fail(h, status_of(e), std::string("batch gather: ") + cudaGetErrorString(e)));
-        int stt = ops_handle_create(&s.h);
+        int stt = OPS_OK;
+        if (!h->spare.empty()) {
+            s.h = h->spare.back();
+            h->spare.pop_back();
+        } else {
+            stt = ops_handle_create(&s.h);
+        }
         if (stt != OPS_OK) return bail(fail(h, stt, "creating a segment handle"));
         s.h->th = h->th;
         int64_t nnz = 0;
@@ -399,10 +411,10 @@ extern "C" int ops_batch_create(ops_handle_t h, int dtype, int32_t count, const 
         s.c_nnz = nnz;
         b->nnz += nnz;
         void *cc = nullptr, *cv = nullptr;
-        e = cudaMalloc(&cc, 4 * (size_t)std::max<int64_t>(nnz, 1));
-        if (e == cudaSuccess) e = cudaMalloc(&cv, vs * (size_t)std::max<int64_t>(nnz, 1));
+        e = cudaMallocFromPoolAsync(&cc, 4 * (size_t)std::max<int64_t>(nnz, 1), h->pool, st);
+        if (e == cudaSuccess) e = cudaMallocFromPoolAsync(&cv, vs * (size_t)std::max<int64_t>(nnz, 1), h->pool, st);
         if (e != cudaSuccess) {
-            if (cc) cudaFree(cc);
+            if (cc) cudaFreeAsync(cc, st);
             return bail(fail(h, status_of(e), "allocating a segment's C"));
         }
         s.c_col = static_cast<int *>(cc);

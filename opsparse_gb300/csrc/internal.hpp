@@ -3,6 +3,7 @@
 #pragma once
 
 #include <string>
+#include <vector>
 
 #include "common.cuh"
 #include "opsparse_gb300.h"
@@ -33,6 +34,9 @@ struct ops_handle_s {
     int device = 0;
     int num_sms = 0;
     cudaMemPool_t pool = nullptr;
+    // segment handles of released batches, taken by the next batch of this handle (their
+    // streams, events and workspaces are made once)
+    std::vector<ops_handle_s *> spare;
     cudaStream_t side[kNumClasses] = {};
     cudaEvent_t ev_fork = nullptr;
     cudaEvent_t ev_join[kNumClasses] = {};

@@ -827,6 +827,7 @@ int ops_handle_destroy(ops_handle_t h)
 {
     if (!h) return OPS_OK;
     cudaDeviceSynchronize();
+    for (ops_handle_s *s : h->spare) ops_handle_destroy(s);
     if (h->ws) cudaFree(h->ws);
     if (h->dense) cudaFree(h->dense);
     if (h->stage) cudaFree(h->stage);

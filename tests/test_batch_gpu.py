@@ -77,3 +77,26 @@ def test_info(cuda):
     assert flop == sum(oracle.flop(a[0], a[1], b[0])[0] for n, a, b in probs)
     assert nnz == sum(len(oracle.spgemm(*a, *b, n)[1]) for n, a, b in probs)
     batch.close()
+
+
+def test_repeated_batches_reuse_pool_and_segment_handles(cuda):
+    """Batches created one after another on one handle take the released batch's pool
+    memory and segment handles, with plain calls on the same handle in between: every C_b
+    still equals the single-call result bit-for-bit, whatever the previous batch's sizes."""
+    h = ops.Handle()
+    single = ops.Handle()
+    for k, (seed, count, hi) in enumerate(((21, 24, 4096), (22, 40, 16384), (21, 24, 4096), (23, 6, 256))):
+        probs = make_batch(count, seed, hi=hi)
+        pairs = [(ops.csr_to_device(*a, n, n), ops.csr_to_device(*b, n, n)) for n, a, b in probs]
+        batch = ops.Batch(h, pairs)
+        batch.execute(k % 2 == 0)
+        batch.check()
+        for i in range(count):
+            rpt, col, val = batch.result(i)
+            s = single.spgemm(*pairs[i]).to_host()
+            assert np.array_equal(rpt, s[0]) and np.array_equal(col, s[1])
+            assert np.array_equal(val.view(np.uint64), s[2].view(np.uint64))
+        batch.close()
+        s = single.spgemm(*pairs[0]).to_host()
+        c = h.spgemm_oneshot(*pairs[0]).to_host()
+        assert np.array_equal(c[1], s[1]) and np.array_equal(c[2].view(np.uint64), s[2].view(np.uint64))
