@@ -853,10 +853,11 @@ __device__ __forceinline__ void window_load_quads(const int *__restrict__ bcol, 
 
 // Column-window count of a row with at most 32 A entries, a lane per A entry.  The lane's
 // B row is read as 16-byte quads, up to kWinQuads in flight, issued together with the
-// loads of its first and last column that give the window: a stencil row takes three
-// dependent round trips to L2 (A's column, B's row extent, B's columns) where reading the
-// window first and the rows after takes five.  Returns false, having marked nothing, when
-// the products do not fit a window of kWinBits columns.
+// loads of its first and last column that give the window: a stencil row (B rows of 27
+// columns) takes three dependent round trips to L2 (A's column, B's row extent, B's
+// columns), where finding the window before reading the B rows takes at least four.
+// Returns false, having marked nothing, when the products do not fit a window of kWinBits
+// columns.
 template <typename T>
 __device__ __forceinline__ bool window_row_short(const SpgemmArgs<T> &g, int r, int a0, int a1, int nnz_b,
                                                  bool bcol16, unsigned *bits, bool &clean,
