@@ -124,7 +124,10 @@ const char *ops_status_string(int status);
  * cols_a x cols_b.  On success *c_rpt, *c_col, *c_val hold device arrays allocated by
  * the library (ops_handle_set_output_malloc says how to release them) and *c_nnz
  * receives nnz(C).  Returns after the result is complete (the stream is synchronized).
- * dtype: OPS_F64 or OPS_F32. */
+ * dtype: OPS_F64 or OPS_F32.  c_col and c_val hold at least nnz(C) entries: where C at
+ * one entry per intermediate product fits 256 MiB (and no row needs the whole-GPU sort),
+ * they are allocated at that size before nnz(C) is known, which spares the call a host
+ * round trip between its counting and numeric phases. */
 int ops_spgemm(ops_handle_t handle, int dtype, int32_t rows_a, int32_t cols_a, int32_t cols_b,
                const int32_t *a_rpt, const int32_t *a_col, const void *a_val, int64_t a_nnz,
                const int32_t *b_rpt, const int32_t *b_col, const void *b_val, int64_t b_nnz,

@@ -65,6 +65,8 @@ struct ops_handle_s {
     void *cub_tmp = nullptr;
     size_t cub_bytes = 0;
     DevInfo *h_info = nullptr;  // pinned host mirror
+    DevInfo *h_info_count = nullptr;  // the counting phase's results, read at the end of a
+                                      // call whose C was allocated before they were known
 
     // dense-row scratch, all-zero between kernels
     unsigned char *dense = nullptr;

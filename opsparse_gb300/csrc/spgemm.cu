@@ -588,7 +588,30 @@ float ev_ms(cudaEvent_t a, cudaEvent_t b)
     return ms;
 }
 
-int run_symbolic(ops_handle_s *h, const Mat &A, const Mat &B, int *c_rpt, long long *c_nnz, cudaStream_t st)
+int dtype_size(int dtype) { return dtype == OPS_F64 ? 8 : (dtype == OPS_F32 ? 4 : 0); }
+
+// Largest C (at one entry per product) that a one-pass ops_spgemm allocates before its
+// entry count is known.
+constexpr long long kEarlyAllocBytes = 256ll << 20;
+
+// Status of the counting phase from its device results.
+int count_status(ops_handle_s *h, const DevInfo &d)
+{
+    if (d.flags & kErrBadColumn) return fail(h, OPS_INVALID_CSR, "B has a column index outside [0, cols)");
+    if (d.flags & kErrProbeLimit) return fail(h, OPS_PROBE_LIMIT, "symbolic hash table overflow");
+    if (d.total_nnz > (unsigned long long)INT_MAX) return fail(h, OPS_INT32_OVERFLOW, "nnz(C) exceeds INT32_MAX");
+    return OPS_OK;
+}
+
+// Counting phase: class sizes (one host sync), the classes' kernels, the row_ptr scan and
+// nnz(C) (a second sync).  early_alloc (ops_spgemm): where C at one entry per product fits
+// kEarlyAllocBytes and no row is a D row, the second sync is left out; *c_nnz is then -1,
+// plan_nnz holds the product count (an upper bound of nnz(C)) and the phase's results
+// reach h_info_count when the stream gets there, for the caller to read after its own
+// sync.  No D row means no kernel indexes memory by a column of B, so the numeric phase
+// may run before a bad column is reported, writing at most one entry per product.
+int run_symbolic(ops_handle_s *h, const Mat &A, const Mat &B, int *c_rpt, long long *c_nnz, cudaStream_t st,
+                 bool early_alloc = false)
 {
     const int M = A.rows;
     OPS_CHECK(ensure_ws(h, std::max(M, 1), st));
@@ -644,14 +667,20 @@ int run_symbolic(ops_handle_s *h, const Mat &A, const Mat &B, int *c_rpt, long l
     size_t cb = h->cub_bytes;
     OPS_CUDA(h, cub::DeviceScan::ExclusiveSum(h->cub_tmp, cb, c_rpt, c_rpt, M + 1, st));
     if (h->timing) OPS_CUDA(h, cudaEventRecord(h->ev_t[4], st));
-    OPS_CUDA(h, cudaMemcpyAsync(h->h_info, h->info, sizeof(DevInfo), cudaMemcpyDeviceToHost, st));
-    OPS_CUDA(h, cudaStreamSynchronize(st));
-    const DevInfo h2 = *h->h_info;
-    if (h2.flags & kErrBadColumn) return fail(h, OPS_INVALID_CSR, "B has a column index outside [0, cols)");
-    if (h2.flags & kErrProbeLimit) return fail(h, OPS_PROBE_LIMIT, "symbolic hash table overflow");
-    if (h2.total_nnz > (unsigned long long)INT_MAX) return fail(h, OPS_INT32_OVERFLOW, "nnz(C) exceeds INT32_MAX");
-    *c_nnz = (long long)h2.total_nnz;
-    h->plan_nnz = (long long)h2.total_nnz;
+    const int vs = h->op_dtype >= 0 ? dtype_size(h->op_dtype) : 0;
+    if (early_alloc && vs > 0 && hi.counts[kClsD] == 0 &&
+        (long long)hi.total_flop * (long long)(4 + vs) <= kEarlyAllocBytes) {
+        OPS_CUDA(h, cudaMemcpyAsync(h->h_info_count, h->info, sizeof(DevInfo), cudaMemcpyDeviceToHost, st));
+        *c_nnz = -1;
+        h->plan_nnz = (long long)hi.total_flop;
+    } else {
+        OPS_CUDA(h, cudaMemcpyAsync(h->h_info, h->info, sizeof(DevInfo), cudaMemcpyDeviceToHost, st));
+        OPS_CUDA(h, cudaStreamSynchronize(st));
+        const DevInfo h2 = *h->h_info;
+        OPS_CHECK(count_status(h, h2));
+        *c_nnz = (long long)h2.total_nnz;
+        h->plan_nnz = (long long)h2.total_nnz;
+    }
     h->plan_arpt = A.rpt;
     h->plan_acol = A.col;
     h->plan_brpt = B.rpt;
@@ -723,8 +752,6 @@ void fill_timings(ops_handle_s *h, bool with_numeric)
         t.total = ev_ms(h->ev_t[0], h->ev_t[4]) * 1e-3;
     }
 }
-
-int dtype_size(int dtype) { return dtype == OPS_F64 ? 8 : (dtype == OPS_F32 ? 4 : 0); }
 
 // Output arrays of ops_spgemm: the handle's pool (stream-ordered) or plain cudaMalloc.
 cudaError_t out_alloc(ops_handle_s *h, void **p, size_t bytes, cudaStream_t st)
@@ -809,6 +836,7 @@ int ops_handle_create(ops_handle_t *out)
         for (int c = 0; c < kNumClasses && e == cudaSuccess; ++c)
             for (int k = 0; k < 2 && e == cudaSuccess; ++k) e = cudaEventCreate(&h->ev_k[ph][c][k]);
     if (e == cudaSuccess) e = cudaMallocHost(reinterpret_cast<void **>(&h->h_info), sizeof(DevInfo));
+    if (e == cudaSuccess) e = cudaMallocHost(reinterpret_cast<void **>(&h->h_info_count), sizeof(DevInfo));
     if (e == cudaSuccess) {
         set_smem_attrs<double>();
         set_smem_attrs<float>();
@@ -848,6 +876,7 @@ int ops_handle_destroy(ops_handle_t h)
             for (int k = 0; k < 2; ++k)
                 if (h->ev_k[ph][c][k]) cudaEventDestroy(h->ev_k[ph][c][k]);
     if (h->h_info) cudaFreeHost(h->h_info);
+    if (h->h_info_count) cudaFreeHost(h->h_info_count);
     if (h->pool) cudaMemPoolDestroy(h->pool);
     (void)cudaGetLastError();
     delete h;
@@ -1029,14 +1058,18 @@ int ops_spgemm(ops_handle_t h, int dtype, int32_t rows_a, int32_t cols_a, int32_
         OPS_CUDA(h, out_alloc(h, &p, sizeof(int) * ((size_t)rows_a + 1), st));
         int *rpt = static_cast<int *>(p);
         long long nnz = 0;
-        int s = run_symbolic(h, A, B, rpt, &nnz, st);
+        int s = run_symbolic(h, A, B, rpt, &nnz, st, true);
         if (s != OPS_OK) {
             out_free(h, rpt, st);
             return s;
         }
+        // nnz < 0: C allocated at one entry per product, its count read after the numeric
+        // phase, with no host round trip between the two phases
+        const bool early = nnz < 0;
+        const long long cap = early ? h->plan_nnz : nnz;
         void *col = nullptr, *val = nullptr;
-        cudaError_t e = out_alloc(h, &col, sizeof(int) * (size_t)std::max(nnz, 1LL), st);
-        if (e == cudaSuccess) e = out_alloc(h, &val, (size_t)vs * (size_t)std::max(nnz, 1LL), st);
+        cudaError_t e = out_alloc(h, &col, sizeof(int) * (size_t)std::max(cap, 1LL), st);
+        if (e == cudaSuccess) e = out_alloc(h, &val, (size_t)vs * (size_t)std::max(cap, 1LL), st);
         if (h->timing && e == cudaSuccess) e = cudaEventRecord(h->ev_t[5], st);
         if (e != cudaSuccess) {
             (void)cudaGetLastError();
@@ -1051,6 +1084,14 @@ int ops_spgemm(ops_handle_t h, int dtype, int32_t rows_a, int32_t cols_a, int32_
             if (e != cudaSuccess) s = fail(h, status_of(e), "event record");
         }
         if (s == OPS_OK) s = check_flags(h, st);
+        if (early) {  // the stream has passed the counting phase's results (a sync above or
+                      // on the error path below); they take precedence over the numeric's
+            if (s != OPS_OK) cudaStreamSynchronize(st);
+            const int sc = count_status(h, *h->h_info_count);
+            if (sc != OPS_OK) s = sc;
+            nnz = (long long)h->h_info_count->total_nnz;
+            h->plan_nnz = nnz;
+        }
         if (s != OPS_OK) {
             out_free(h, val, st);
             out_free(h, col, st);
