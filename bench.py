@@ -165,17 +165,45 @@ def _pair(data):
 
 
 def cpu_baseline(data, n, steps=3):
+    """Median time of the oracle's OpenMP port on the workload, its thread count, and its
+    result (the checker of the GPU result's parity)."""
     import oracle
 
     (ar, ac, av), (br, bc, bv) = _pair(data)
     av64, bv64 = np.asarray(av, dtype=np.float64), np.asarray(bv, dtype=np.float64)
-    oracle.omp_spgemm(ar, ac, av64, br, bc, bv64)  # warm-up
+    ref = oracle.omp_spgemm(ar, ac, av64, br, bc, bv64)  # warm-up
     ts = []
     for _ in range(steps):
         t0 = time.perf_counter()
         oracle.omp_spgemm(ar, ac, av64, br, bc, bv64)
         ts.append(time.perf_counter() - t0)
-    return statistics.median(ts), oracle.num_threads()
+    return statistics.median(ts), oracle.num_threads(), ref
+
+
+def parity_report(gpu, ref, dt):
+    """Measured error of a GPU result (row_ptr, col_idx, values) against the oracle's FP64
+    result on the same inputs: whether the structure is identical, the largest absolute
+    error, and the largest relative error over the entries the oracle makes nonzero (the
+    ones it makes zero must be zero).  FP64 results are also compared bit for bit."""
+    g_rpt, g_col, g_val = (np.asarray(x) for x in gpu)
+    o_rpt, o_col, o_val = (np.asarray(x) for x in ref)
+    same = (g_rpt.shape == o_rpt.shape and np.array_equal(g_rpt.astype(np.int64), o_rpt.astype(np.int64))
+            and g_col.shape == o_col.shape and np.array_equal(g_col, o_col))
+    rep = {"checked_against": "oracle (FP64, every entry folded in ascending j)", "structure_identical": bool(same),
+           "tolerance_rel": 1e-12 if dt == "f64" else 1e-5}
+    if not same:
+        return rep
+    gv, ov = g_val.astype(np.float64), o_val.astype(np.float64)
+    diff = np.abs(gv - ov)
+    nz = ov != 0
+    rep["entries"] = int(ov.size)
+    rep["max_abs_err"] = float(diff.max()) if diff.size else 0.0
+    rep["max_rel_err"] = float((diff[nz] / np.abs(ov[nz])).max()) if nz.any() else 0.0
+    rep["zeros_exact"] = bool(np.all(gv[~nz] == 0))
+    if dt == "f64":
+        rep["values_bit_identical"] = bool(np.array_equal(gv.view(np.uint64), ov.view(np.uint64)))
+    rep["within_tolerance"] = bool(rep["max_rel_err"] <= rep["tolerance_rel"] and rep["zeros_exact"])
+    return rep
 
 
 def run_reference(args, desc, dt, data, n, rank, world):
@@ -439,10 +467,16 @@ def run_ours(args, desc, dt, data, n, rank, world, local_rank):
     if world == 1 and args.cusparse:
         line["cusparse_gpu"] = cusparse_gpu(A, B, n, P, nnz_c, t_ms, flush)
     if args.cpu_baseline and world == 1:
-        t_cpu, cores = cpu_baseline(data, n)
+        t_cpu, cores, ref = cpu_baseline(data, n)
         line["cpu_baseline"] = {"value": 2.0 * P / t_cpu / 1e9, "unit": "GFLOPS", "cores": cores, "kind": "port",
                                 "sample": "full workload, median of 3 runs after 1 warm-up, FP64, OpenMP row-wise "
                                           "hash Gustavson on the host cores"}
+        # the last end-to-end step's C (in the pinned host buffers) against the baseline's
+        try:
+            gpu_c = (h_out[0][:n + 1].numpy(), h_out[1][:nnz_c].numpy(), h_out[2][:nnz_c].numpy())
+            line["parity"] = parity_report(gpu_c, ref, dt)
+        except Exception as exc:  # a report, never a reason to lose the measurement
+            line["parity"] = {"error": f"{type(exc).__name__}: {exc}"}
     h.close()
     print(json.dumps(line), flush=True)
 
