@@ -180,17 +180,24 @@ def cpu_baseline(data, n, steps=3):
     return statistics.median(ts), oracle.num_threads(), ref
 
 
-def parity_report(gpu, ref, dt):
+def parity_report(gpu, ref, dt, scale_fn=None):
     """Measured error of a GPU result (row_ptr, col_idx, values) against the oracle's FP64
     result on the same inputs: whether the structure is identical, the largest absolute
-    error, and the largest relative error over the entries the oracle makes nonzero (the
-    ones it makes zero must be zero).  FP64 results are also compared bit for bit."""
+    error, and the largest relative error over the entries the oracle makes nonzero.
+
+    FP64 results are also compared bit for bit, and the entries the oracle makes zero must
+    be zero.  FP32 results are rounded sums of FP32 products: an entry whose terms cancel
+    carries an error of the order of 2^-24 * sum_j |a_ij b_jk| however small the entry, so
+    for FP32 each error is also taken relative to max(|c_ik|, 2^-24 * sum_j |a_ij b_jk|)
+    (`max_rel_err_scaled`; the sums come from scale_fn(), called only when some entry
+    misses the plain relative bound), and that figure decides the tolerance."""
     g_rpt, g_col, g_val = (np.asarray(x) for x in gpu)
     o_rpt, o_col, o_val = (np.asarray(x) for x in ref)
     same = (g_rpt.shape == o_rpt.shape and np.array_equal(g_rpt.astype(np.int64), o_rpt.astype(np.int64))
             and g_col.shape == o_col.shape and np.array_equal(g_col, o_col))
+    tol = 1e-12 if dt == "f64" else 1e-5
     rep = {"checked_against": "oracle (FP64, every entry folded in ascending j)", "structure_identical": bool(same),
-           "tolerance_rel": 1e-12 if dt == "f64" else 1e-5}
+           "tolerance_rel": tol}
     if not same:
         return rep
     gv, ov = g_val.astype(np.float64), o_val.astype(np.float64)
@@ -202,7 +209,18 @@ def parity_report(gpu, ref, dt):
     rep["zeros_exact"] = bool(np.all(gv[~nz] == 0))
     if dt == "f64":
         rep["values_bit_identical"] = bool(np.array_equal(gv.view(np.uint64), ov.view(np.uint64)))
-    rep["within_tolerance"] = bool(rep["max_rel_err"] <= rep["tolerance_rel"] and rep["zeros_exact"])
+        rep["within_tolerance"] = bool(rep["max_rel_err"] <= tol and rep["zeros_exact"])
+        return rep
+    plain_ok = rep["max_rel_err"] <= tol and rep["zeros_exact"]
+    if plain_ok or scale_fn is None:
+        rep["max_rel_err_scaled"] = rep["max_rel_err"] if rep["zeros_exact"] else None
+        rep["within_tolerance"] = bool(plain_ok)
+        return rep
+    den = np.maximum(np.abs(ov), np.asarray(scale_fn(), dtype=np.float64) * 2.0 ** -24)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        rel = np.where(den > 0, diff / np.where(den > 0, den, 1.0), np.where(diff > 0, np.inf, 0.0))
+    rep["max_rel_err_scaled"] = float(rel.max()) if rel.size else 0.0
+    rep["within_tolerance"] = bool(rep["max_rel_err_scaled"] <= tol)
     return rep
 
 
@@ -306,7 +324,11 @@ def reference_gpu(A, B, n, P, nnz_c, t_ms, flush, iters=10):
             "speedup_of_this_library": mean["total"] / t_ms}
 
 
-def run_ours(args, desc, dt, data, n, rank, world, local_rank):
+def measure_plain(args, desc, dt, data, n, world, local_rank, steps, warmup, side=True):
+    """One plain workload through the C-ABI call ops_spgemm: K timed steps on device-resident
+    inputs, then K end-to-end steps with host buffers.  Returns the bench-line fields; with
+    side=True (rank 0 of a one-GPU run) also OpSparse's kernels and cuSPARSE on the same
+    inputs, the CPU baseline and the measured error of the last end-to-end result."""
     import torch
 
     import opsparse_gb300 as ops
@@ -341,7 +363,7 @@ def run_ours(args, desc, dt, data, n, rank, world, local_rank):
             lib.ops_free(p, st)
 
     # untimed warm-up; also collect phase and per-class kernel times
-    for _ in range(max(args.warmup, 3)):
+    for _ in range(max(warmup, 3)):
         release(step())
     h.set_timing(2)
     out = step()
@@ -353,13 +375,13 @@ def run_ours(args, desc, dt, data, n, rank, world, local_rank):
     P = int(phases["flop"])
 
     # timed region: K steps, L2 flushed between steps outside the events
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
     launches = 0
     with ClockSampler(local_rank) as clk:
-        for i in range(args.steps):
+        for i in range(steps):
             flush.zero_()
             ev[i][0].record(stream)
             out = step()
@@ -403,7 +425,7 @@ def run_ours(args, desc, dt, data, n, rank, world, local_rank):
 
     vstr = "<f8" if dt == "f64" else "<f4"
     e2e_ms = []
-    for i in range(args.warmup + args.steps):
+    for i in range(warmup + steps):
         flush.zero_()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
@@ -425,13 +447,11 @@ def run_ours(args, desc, dt, data, n, rank, world, local_rank):
         e1.record(stream)
         torch.cuda.synchronize()
         release((rp2, cp2, vp2))
-        if i >= args.warmup:
+        if i >= warmup:
             e2e_ms.append(e0.elapsed_time(e1))
     e2e_t = max_over_ranks(float(np.mean(e2e_ms)), world, dev)
     e2e_gf = world * 2.0 * P / (e2e_t * 1e-3) / 1e9
 
-    if rank != 0:
-        return
     peak, peak_kind = measured_peak()
     nnz_a = len(col)
     balg = bytes_alg(n, n, nnz_a, len(bcol), nnz_c, s)
@@ -442,9 +462,7 @@ def run_ours(args, desc, dt, data, n, rank, world, local_rank):
     per_kernel = {f"{ph}_{names[c]}": round(kms[i][c], 4) for i, ph in enumerate(("symbolic", "numeric"))
                   for c in range(7) if kms[i][c] > 0}
     line = {
-        "metric": METRIC, "value": gflops, "unit": "GFLOPS", "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": t_ms, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": dt, "data": "synthetic (seeded stand-in for the SuiteSparse inputs)",
+        "value": gflops, "unit": "GFLOPS", "steps": steps, "warmup": warmup, "ms_per_step": t_ms, "dtype": dt,
         "config": dict(desc, l2="flushed between steps (256 MiB write outside the timed events)",
                        products=P, nnz_a=nnz_a, nnz_c=nnz_c, parallelism=f"replica x{world}",
                        short_rows="one pass" if args.one_pass else "two passes"),
@@ -462,11 +480,11 @@ def run_ours(args, desc, dt, data, n, rank, world, local_rank):
         "gpu_launches": launches,
         "clocks": clk.summary(),
     }
-    if dt == "f64" and world == 1 and args.reference_gpu:
+    if side and dt == "f64" and world == 1 and args.reference_gpu:
         line["reference_gpu"] = reference_gpu(A, B, n, P, nnz_c, t_ms, flush)
-    if world == 1 and args.cusparse:
+    if side and world == 1 and args.cusparse:
         line["cusparse_gpu"] = cusparse_gpu(A, B, n, P, nnz_c, t_ms, flush)
-    if args.cpu_baseline and world == 1:
+    if side and args.cpu_baseline and world == 1:
         t_cpu, cores, ref = cpu_baseline(data, n)
         line["cpu_baseline"] = {"value": 2.0 * P / t_cpu / 1e9, "unit": "GFLOPS", "cores": cores, "kind": "port",
                                 "sample": "full workload, median of 3 runs after 1 warm-up, FP64, OpenMP row-wise "
@@ -474,11 +492,67 @@ def run_ours(args, desc, dt, data, n, rank, world, local_rank):
         # the last end-to-end step's C (in the pinned host buffers) against the baseline's
         try:
             gpu_c = (h_out[0][:n + 1].numpy(), h_out[1][:nnz_c].numpy(), h_out[2][:nnz_c].numpy())
-            line["parity"] = parity_report(gpu_c, ref, dt)
+            line["parity"] = parity_report(gpu_c, ref, dt, scale_fn=_abs_sums_fn(data))
         except Exception as exc:  # a report, never a reason to lose the measurement
             line["parity"] = {"error": f"{type(exc).__name__}: {exc}"}
     h.close()
-    print(json.dumps(line), flush=True)
+    del A, B, flush, d_in, pin, h_out
+    torch.cuda.empty_cache()
+    return line
+
+
+def _abs_sums_fn(data):
+    """sum_j |a_ij b_jk| per output entry of a workload (the OpenMP port over |A| and |B|,
+    whose output has C's structure): the scale of FP32 rounding in cancelling entries."""
+    def f():
+        import oracle
+
+        (ar, ac, av), (br, bc, bv) = _pair(data)
+        return oracle.omp_spgemm(ar, ac, np.abs(np.asarray(av, dtype=np.float64)), br, bc,
+                                 np.abs(np.asarray(bv, dtype=np.float64)))[2]
+
+    return f
+
+
+def run_ours(args, desc, dt, data, n, rank, world, local_rank):
+    line = measure_plain(args, desc, dt, data, n, world, local_rank, args.steps, args.warmup, side=(rank == 0))
+    line = {"metric": METRIC, "value": line.pop("value"), "unit": line.pop("unit"), "n_gpus": world,
+            "steps": line.pop("steps"), "warmup": line.pop("warmup"), "ms_per_step": line.pop("ms_per_step"),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": line.pop("dtype"),
+            "data": "synthetic (seeded stand-in for the SuiteSparse inputs)", **line}
+    if world == 1 and args.configs and args.workload == "web":
+        line["configs"] = other_configs(args, local_rank)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def other_configs(args, local_rank):
+    """The benchmark's other configurations, measured in the same run as the headline: the
+    Laplacian, the 27-point stencil in FP64 and FP32 and the A*A^T power-law forward (each
+    as the headline: device and end-to-end time, roofline, CPU baseline, measured error,
+    OpSparse's kernels and cuSPARSE on the same GPU), the 4,096-problem batch against the
+    per-call loop, and forward + backward against the forward.  Fewer steps for the heavy
+    legs; each entry states its own."""
+    out = {}
+    for name, wl, steps in (("C1", "laplacian", args.steps), ("C3_f64", "stencil27", max(3, args.steps // 2)),
+                            ("C3_f32", "stencil27_f32", max(3, args.steps // 2)),
+                            ("C5_forward_f64", "powerlaw_AAt", max(3, args.steps // 2))):
+        try:
+            desc, dt, data, n = make_workload(wl)
+            out[name] = measure_plain(args, desc, dt, data, n, 1, local_rank, steps, 3, side=True)
+        except Exception as exc:  # one configuration failing must not lose the others
+            out[name] = {"error": f"{type(exc).__name__}: {exc}"}
+    try:
+        out["C4_batched"] = measure_batched(args, local_rank, args.batch, reps_loop=2, reps_batch=2,
+                                            reps_replay=max(3, args.steps // 2))
+    except Exception as exc:
+        out["C4_batched"] = {"error": f"{type(exc).__name__}: {exc}"}
+    for name, dtn in (("C5_fwd_bwd_f64", "f64"), ("C5_fwd_bwd_f32", "f32")):
+        try:
+            out[name] = measure_backward(local_rank, dtn, steps=max(3, args.steps // 2), warmup=3)
+        except Exception as exc:
+            out[name] = {"error": f"{type(exc).__name__}: {exc}"}
+    return out
 
 
 def main():
@@ -498,6 +572,9 @@ def main():
                     help="count and compute every row in separate passes (no staging of short rows)")
     ap.add_argument("--no-reference-gpu", dest="reference_gpu", action="store_false",
                     help="skip timing OpSparse's own kernels on the GPU (for profiling runs)")
+    ap.add_argument("--no-configs", dest="configs", action="store_false",
+                    help="measure the chosen workload only (by default the headline run also measures the other "
+                         "configurations, the batch and forward+backward, reported under 'configs')")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -534,22 +611,35 @@ def run_plain(args, desc, dt, data, n, rank, world, local_rank):
 
 
 # ------------------------------------------------------------------- batched workload
-def run_batched(args, rank, world, local_rank):
-    """4,096 independent FP32 Erdos-Renyi products (sizes log-uniform in 64..65,536, mean
-    degree U(4,32)): per-call loop of ops_spgemm vs one planned batch (ops_batch_create +
-    ops_batch_execute) and vs graph replays of the planned numeric phase."""
+def _timed(fn, reps, stream=None):
+    """Median of `reps` CUDA-event times of fn() (synchronized on both sides)."""
+    import torch
+
+    ts = []
+    for _ in range(reps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ts.append(e0.elapsed_time(e1))
+    return float(np.median(ts))
+
+
+def measure_batched(args, local_rank, count, reps_loop, reps_batch, reps_replay, sample=8):
+    """`count` independent FP32 Erdos-Renyi products (sizes log-uniform in 64..65,536, mean
+    degree U(4,32), generated on the device): the per-call loop of ops_spgemm against one
+    batch (ops_batch_create + ops_batch_execute, every problem planned and computed) and
+    against graph replays of the planned numeric phase; a seeded sample of the batch's
+    results against the oracle."""
     import torch
 
     import opsparse_gb300 as ops
     from opsparse_gb300 import capi, gen_device
 
-    if args.impl == "reference":  # answered without touching a GPU
-        if rank == 0:
-            print(json.dumps({"metric": METRIC, "impl": "reference", "unavailable":
-                              "OpSparse has no batched SpGEMM and no CPU SpGEMM; see the plain workloads"}))
-        return
     torch.cuda.set_device(local_rank)
-    sizes, row_base, a_side, b_side = gen_device.er_batch(args.batch, dtype=torch.float32)
+    sizes, row_base, a_side, b_side = gen_device.er_batch(count, dtype=torch.float32)
     A = gen_device.problem_slices(sizes, row_base, a_side)
     B = gen_device.problem_slices(sizes, row_base, b_side)
     pairs = []
@@ -570,21 +660,9 @@ def run_batched(args, rank, world, local_rank):
             for p_ in (rp, cp, vp):
                 lib.ops_free(p_, st)
 
-    def timed(fn, reps):
-        ts = []
-        for _ in range(reps):
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            torch.cuda.synchronize()
-            e0.record(stream)
-            fn()
-            e1.record(stream)
-            torch.cuda.synchronize()
-            ts.append(e0.elapsed_time(e1))
-        return float(np.median(ts))
-
     with torch.cuda.stream(stream):
         loop_once()  # warm-up
-        loop_ms = timed(loop_once, max(1, args.steps // 4))
+        loop_ms = _timed(loop_once, reps_loop, stream)
         holder = {}
 
         def batched_full():
@@ -594,43 +672,78 @@ def run_batched(args, rank, world, local_rank):
             holder["b"].execute(False)
 
         batched_full()
-        full_ms = timed(batched_full, max(1, args.steps // 4))
+        full_ms = _timed(batched_full, reps_batch, stream)
         bt = holder["b"]
         bt.execute(True)  # records the graph
-        replay_ms = timed(lambda: bt.execute(True), args.steps)
+        replay_ms = _timed(lambda: bt.execute(True), reps_replay, stream)
+    bt.check()
     seg, flop, nnz = bt.info()
-    gf = 2.0 * flop / (full_ms * 1e-3) / 1e9
-    line = {"metric": METRIC, "value": gf, "unit": "GFLOPS", "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": full_ms, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32", "data": "synthetic (device-generated Erdos-Renyi pairs)",
-            "config": {"workload": f"batched_er_{args.batch}", "problems": args.batch, "sizes": "log-uniform 64..65536",
-                       "mean_degree": "U(4,32)", "values": "N(0,1)", "products": flop, "nnz_c": nnz,
-                       "segments": seg},
-            "batched": {"loop_ms": loop_ms, "batched_ms": full_ms, "speedup_vs_loop": loop_ms / full_ms,
-                        "graph_replay_numeric_ms": replay_ms}}
+    # measured error of a seeded sample of the batch's results
+    par = {"problems_checked": 0, "structure_identical": True, "within_tolerance": True, "max_abs_err": 0.0,
+           "max_rel_err_scaled": 0.0, "entries": 0, "values_bit_identical_to_fp32_oracle": True,
+           "tolerance_rel": 1e-5, "checked_against": "oracle (FP64; and FP32 Dot2 for bit identity)"}
+    if args.cpu_baseline and sample:
+        import oracle
+
+        for i in np.random.default_rng(20261203).choice(len(pairs), min(sample, len(pairs)), replace=False):
+            Ap, Bp = pairs[int(i)]
+            a = tuple(x.cpu().numpy() for x in (Ap.rpt, Ap.col, Ap.val))
+            b = tuple(x.cpu().numpy() for x in (Bp.rpt, Bp.col, Bp.val))
+            gpu = bt.result(int(i))
+            ref32 = oracle.spgemm(*a, *b, Bp.cols, dtype=np.float32)
+            ref64 = oracle.spgemm(a[0], a[1], a[2].astype(np.float64), b[0], b[1], b[2].astype(np.float64), Bp.cols)
+            rep = parity_report(gpu, ref64, "f32", scale_fn=_abs_sums_fn((a, b)))
+            par["problems_checked"] += 1
+            par["structure_identical"] &= bool(rep["structure_identical"])
+            par["within_tolerance"] &= bool(rep.get("within_tolerance", False))
+            par["max_abs_err"] = max(par["max_abs_err"], rep.get("max_abs_err", float("inf")))
+            par["max_rel_err_scaled"] = max(par["max_rel_err_scaled"], rep.get("max_rel_err_scaled") or 0.0)
+            par["entries"] += rep.get("entries", 0)
+            par["values_bit_identical_to_fp32_oracle"] &= bool(
+                np.array_equal(gpu[2].view(np.uint32), ref32[2].view(np.uint32)))
     bt.close()
+    h.close()
+    del pairs, A, B, a_side, b_side
+    torch.cuda.empty_cache()
+    return {"value": 2.0 * flop / (full_ms * 1e-3) / 1e9, "unit": "GFLOPS", "dtype": "f32",
+            "ms_per_step": full_ms,
+            "config": {"workload": f"batched_er_{count}", "problems": count, "sizes": "log-uniform 64..65536",
+                       "mean_degree": "U(4,32)", "values": "N(0,1)", "products": flop, "nnz_c": nnz,
+                       "segments": seg, "data": "synthetic (device-generated Erdos-Renyi pairs)"},
+            "batched": {"loop_ms": loop_ms, "batched_ms": full_ms, "speedup_vs_loop": loop_ms / full_ms,
+                        "graph_replay_numeric_ms": replay_ms, "target_speedup": 3.0,
+                        "reps": {"loop": reps_loop, "batched": reps_batch, "replay": reps_replay}},
+            "parity": par}
+
+
+def run_batched(args, rank, world, local_rank):
+    if args.impl == "reference":  # answered without touching a GPU
+        if rank == 0:
+            print(json.dumps({"metric": METRIC, "impl": "reference", "unavailable":
+                              "OpSparse has no batched SpGEMM and no CPU SpGEMM; see the plain workloads"}))
+        return
+    r = measure_batched(args, local_rank, args.batch, max(1, args.steps // 4), max(1, args.steps // 4), args.steps)
+    line = {"metric": METRIC, "value": r.pop("value"), "unit": r.pop("unit"), "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": r.pop("ms_per_step"), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": r.pop("dtype"), "data": r["config"].pop("data"), **r}
     if rank == 0:
         print(json.dumps(line), flush=True)
 
 
 # ----------------------------------------------------------------- backward workload
-def run_backward(args, rank, world, local_rank):
+def measure_backward(local_rank, dtn, steps, warmup):
     """C = A*B with A 200,000^2 power-law (mean degree 16, exponent 2.2) and B = pattern of
     A^T with fresh values; loss = sum(W .* C).  Times the forward (numeric phase on the
-    fixed pattern, and the full SpGEMM) and forward + backward (dA, dB)."""
+    fixed pattern, and the full SpGEMM) and forward + backward (dA, dB); measures the
+    gradients' error against the oracle's backward."""
     import torch
 
     import opsparse_gb300 as ops
     from opsparse_gb300 import gen
     from opsparse_gb300.autograd import FixedPatternSpGEMM
 
-    if args.impl == "reference":  # answered without touching a GPU
-        if rank == 0:
-            print(json.dumps({"metric": METRIC, "impl": "reference", "unavailable":
-                              "OpSparse has no backward pass; see the plain workloads"}))
-        return
     torch.cuda.set_device(local_rank)
-    dt = torch.float32 if args.workload.endswith("f32") else torch.float64
+    dt = torch.float32 if dtn == "f32" else torch.float64
     n = 200_000
     a = gen.powerlaw_square(n, 16, 2.2)
     b = gen.transpose_pattern(a[0], a[1], n)
@@ -638,41 +751,67 @@ def run_backward(args, rank, world, local_rank):
     B = ops.csr_to_device(*b, n, n, dtype=dt)
     h = ops.Handle()
     op = FixedPatternSpGEMM(A, B, h)
-    w = torch.randn(op.nnz, dtype=dt, device="cuda")
+    w = torch.as_tensor(np.random.default_rng(3).standard_normal(op.nnz)).to(dt).cuda()
     flop = int(gen.row_flop(a[0], a[1], b[0]).sum())
-
-    def timed(fn, reps):
-        ts = []
-        for _ in range(reps):
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            torch.cuda.synchronize()
-            e0.record()
-            fn()
-            e1.record()
-            torch.cuda.synchronize()
-            ts.append(e0.elapsed_time(e1))
-        return float(np.median(ts))
-
     fwd = lambda: op.forward_values(A.val, B.val)  # noqa: E731
     fwdbwd = lambda: (op.forward_values(A.val, B.val), op.backward_values(A.val, B.val, w))  # noqa: E731
     full = lambda: h.spgemm_oneshot(A, B)  # noqa: E731
-    for _ in range(max(args.warmup, 3)):
+    for _ in range(max(warmup, 3)):
         fwdbwd()
         full()
-    fwd_ms = timed(fwd, args.steps)
-    fwdbwd_ms = timed(fwdbwd, args.steps)
-    full_ms = timed(full, args.steps)
+    fwd_ms = _timed(fwd, steps)
+    fwdbwd_ms = _timed(fwdbwd, steps)
+    full_ms = _timed(full, steps)
     products, with_map = op.plan_info()
-    line = {"metric": METRIC, "value": 2.0 * flop / (fwdbwd_ms * 1e-3) / 1e9, "unit": "GFLOPS", "n_gpus": world,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": fwdbwd_ms, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64" if dt == torch.float64 else "f32",
-            "data": "synthetic", "config": {"workload": "powerlaw_200k_AAt_fwd_bwd", "rows": n, "mean_degree": 16,
-                                            "exponent": 2.2, "products": flop, "nnz_c": op.nnz},
+    # gradients against the oracle's FP64 backward on the same (rounded) inputs
+    da, db = op.backward_values(A.val, B.val, w)
+    grad = {}
+    try:
+        import oracle
+
+        av, bv, wv = (x.cpu().numpy().astype(np.float64) for x in (A.val, B.val, w))
+        crpt, ccol = op.c_rpt.cpu().numpy().astype(np.int64), op.c_col.cpu().numpy()
+        oda, odb = oracle.backward(a[0], a[1], av, b[0], b[1], bv, n, crpt, ccol, wv)
+        sda, sdb = oracle.backward(a[0], a[1], np.abs(av), b[0], b[1], np.abs(bv), n, crpt, ccol, np.abs(wv))
+        for nm, g, o, sc in (("dA", da, oda, sda), ("dB", db, odb, sdb)):
+            g = g.cpu().numpy()
+            diff = np.abs(g.astype(np.float64) - o)
+            den = np.maximum(np.abs(o), sc * (2.0 ** -24 if dtn == "f32" else 2.0 ** -53))
+            rel = np.where(den > 0, diff / np.where(den > 0, den, 1.0), np.where(diff > 0, np.inf, 0.0))
+            e = {"entries": int(o.size), "max_abs_err": float(diff.max()) if diff.size else 0.0,
+                 "max_rel_err_scaled": float(rel.max()) if rel.size else 0.0,
+                 "tolerance_rel": 1e-12 if dtn == "f64" else 1e-5}
+            if dtn == "f64":
+                e["values_bit_identical"] = bool(np.array_equal(g.view(np.uint64), o.view(np.uint64)))
+            e["within_tolerance"] = bool(e["max_rel_err_scaled"] <= e["tolerance_rel"])
+            grad[nm] = e
+    except Exception as exc:  # a report, never a reason to lose the measurement
+        grad = {"error": f"{type(exc).__name__}: {exc}"}
+    nnz_c = int(op.nnz)
+    h.close()
+    del A, B, op, w
+    torch.cuda.empty_cache()
+    return {"value": 2.0 * flop / (fwdbwd_ms * 1e-3) / 1e9, "unit": "GFLOPS", "dtype": dtn, "steps": steps,
+            "ms_per_step": fwdbwd_ms,
+            "config": {"workload": "powerlaw_200k_AAt_fwd_bwd", "rows": n, "mean_degree": 16, "exponent": 2.2,
+                       "products": flop, "nnz_c": nnz_c},
             "fwd_bwd": {"forward_numeric_ms": fwd_ms, "forward_full_ms": full_ms, "fwd_bwd_ms": fwdbwd_ms,
                         "ratio_vs_numeric_forward": fwdbwd_ms / fwd_ms,
-                        "ratio_vs_full_forward": (fwdbwd_ms - fwd_ms + full_ms) / full_ms,
-                        "product_map": with_map}}
-    h.close()
+                        "ratio_vs_full_forward": (fwdbwd_ms - fwd_ms + full_ms) / full_ms, "target_ratio": 3.0,
+                        "product_map": with_map},
+            "gradient_error": grad}
+
+
+def run_backward(args, rank, world, local_rank):
+    if args.impl == "reference":  # answered without touching a GPU
+        if rank == 0:
+            print(json.dumps({"metric": METRIC, "impl": "reference", "unavailable":
+                              "OpSparse has no backward pass; see the plain workloads"}))
+        return
+    r = measure_backward(local_rank, "f32" if args.workload.endswith("f32") else "f64", args.steps, args.warmup)
+    line = {"metric": METRIC, "value": r.pop("value"), "unit": r.pop("unit"), "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": r.pop("ms_per_step"), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": r.pop("dtype"), "data": "synthetic", **r}
     if rank == 0:
         print(json.dumps(line), flush=True)
 

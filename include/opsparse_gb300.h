@@ -227,14 +227,14 @@ int ops_tuning_lookup(const char *path, const char *key, int32_t *thresholds);
 int ops_flop(int32_t rows_a, int32_t cols_a, const int32_t *a_rpt, const int32_t *a_col, const int32_t *b_rpt,
              int64_t *row_flop, int64_t *total, void *stream);
 
-/* ops_flop without any device allocation, for callers that may not allocate at this point:
- * a CUDA graph being captured that must not gain allocation nodes, serving loops that
- * forbid the CUDA allocator after start-up, fixed-budget hosts.  Same arguments and
- * results as ops_flop.  Its scratch is a 64 KiB array in the library's own device memory,
- * shared by every call: rows_a above 2,097,152 returns OPS_NOT_SUPPORTED; calls that
- * overlap on the GPU race and must be serialized; the first call on a device resolves the
- * array's address and should come before any stream capture.  Synchronizes the stream.
- * No counterpart in OpSparse. */
+/* ops_flop without any device allocation, for callers that may not allocate device memory
+ * at this point: serving loops that forbid the CUDA allocator once running, hosts that give
+ * the library a fixed memory budget.  Same arguments and results as ops_flop.  Its scratch
+ * is a 64 KiB array in the library's own device memory, shared by every call: rows_a above
+ * 2,097,152 returns OPS_NOT_SUPPORTED; calls that overlap on the GPU race and must be
+ * serialized; the first call on a device resolves the array's address (keep that call
+ * before any stream capture, and do not use the library across cudaDeviceReset).
+ * Synchronizes the stream.  No counterpart in OpSparse. */
 int ops_flop_noalloc(int32_t rows_a, int32_t cols_a, const int32_t *a_rpt, const int32_t *a_col,
                      const int32_t *b_rpt, int64_t *row_flop, int64_t *total, void *stream);
 

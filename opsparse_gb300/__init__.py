@@ -259,6 +259,23 @@ class Batch:
                               device="cuda").cpu().numpy()
         return rpt, col, val
 
+    def result_device(self, i: int):
+        """(rpt, col, val, nnz) of C_i as torch views of the batch's device storage (valid
+        until close())."""
+        torch = _torch()
+        rp, cp, vp, nnz = C.c_void_p(), C.c_void_p(), C.c_void_p(), C.c_int64(0)
+        check(self.lib.ops_batch_result(self.b, i, C.byref(rp), C.byref(cp), C.byref(vp), C.byref(nnz)), self.h.h)
+        A = self.pairs[i][0]
+        n = int(nnz.value)
+        dev = A.rpt.device
+        vstr = "<f8" if self.dtype == torch.float64 else "<f4"
+        rpt = torch.as_tensor(_DevArray(rp.value, A.rows + 1, "<i4"), device=dev)
+        if n == 0:
+            return rpt, torch.empty(0, dtype=torch.int32, device=dev), torch.empty(0, dtype=self.dtype, device=dev), 0
+        col = torch.as_tensor(_DevArray(cp.value, n, "<i4"), device=dev)
+        val = torch.as_tensor(_DevArray(vp.value, n, vstr), device=dev)
+        return rpt, col, val, n
+
     def close(self):
         if getattr(self, "b", None):
             self.lib.ops_batch_destroy(self.b)

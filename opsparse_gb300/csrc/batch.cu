@@ -290,7 +290,7 @@ extern "C" int ops_batch_create(ops_handle_t h, int dtype, int32_t count, const 
         if (e != cudaSuccess) return bail(fail(h, status_of(e), "allocating batch descriptors"));
         b->d_items = static_cast<Item *>(p);
         void *f = nullptr;
-        e = cudaMallocAsync(&f, sizeof(unsigned long long) * std::max(count, 1), st);
+        e = cudaMallocFromPoolAsync(&f, sizeof(unsigned long long) * std::max(count, 1), h->pool, st);
         if (e == cudaSuccess) e = cudaMemcpyAsync(b->d_items, b->items.data(), sizeof(Item) * count, cudaMemcpyHostToDevice, st);
         if (e == cudaSuccess) e = cudaMemsetAsync(f, 0, sizeof(unsigned long long) * std::max(count, 1), st);
         if (e == cudaSuccess && count > 0 && total_a > 0) {

@@ -27,33 +27,54 @@ void SpgemmTimings::operator/=(double x)
 #undef DIV_FIELD
 }
 
+// Same text as OpSparse's SpgemmTimings::print (src/opsparse/profile/spgemm_timings.cpp:35-70),
+// so logs and scripts that read it keep working: the four phases it highlights keep their
+// ANSI colour, the shares divide by `total`, and GFLOPS divide by each phase's time (inf
+// for a phase this library does not have, as there).
 void SpgemmTimings::print(double total_flop) const
 {
     const double g = total_flop / 1e9;
     std::printf("total flop %lf\n", total_flop);
     if (!measure_separate) return;
+    const double sum_total =
+        setup + symbolic_binning + symbolic + numeric_binning + reduce + prefix + allocate + numeric + cleanup;
+    struct Row {
+        const char *label;
+        double v;
+        bool red;
+    };
+    const Row rows[] = {{"setup           ", setup, false},     {"symbolic_binning", symbolic_binning, true},
+                        {"symbolic        ", symbolic, true},   {"reduce           ", reduce, false},
+                        {"numeric_binning ", numeric_binning, true}, {"prefix          ", prefix, false},
+                        {"allocate        ", allocate, false},  {"numeric         ", numeric, true},
+                        {"cleanup         ", cleanup, false},   {"sum_total       ", sum_total, false},
+                        {"total           ", total, false}};
     std::printf("time(ms):\n");
-#define PRINT_MS(f) std::printf("    %-16s %8.3lfms %6.2lf%%\n", #f, 1000 * f, total > 0 ? f / total * 100 : 0.0);
-    OPSPARSE_TIMING_FIELDS(PRINT_MS)
-#undef PRINT_MS
+    for (const Row &r : rows) {
+        if (r.red) std::printf("\e[1;31m    %s %8.3lfms %6.2lf%%\n\e[0m", r.label, 1000 * r.v, r.v / total * 100);
+        else std::printf("    %s %8.3lfms %6.2lf%%\n", r.label, 1000 * r.v, r.v / total * 100);
+    }
     std::printf("perf(Gflops):\n");
-#define PRINT_GF(f) std::printf("    %-16s %6.2lf\n", #f, f > 0 ? g / f : 0.0);
-    OPSPARSE_TIMING_FIELDS(PRINT_GF)
-#undef PRINT_GF
+    const Row perf[] = {{"setup           ", setup, false},    {"symbolic_binning", symbolic_binning, false},
+                        {"symbolic        ", symbolic, false}, {"reduce          ", reduce, false},
+                        {"numeric_binning ", numeric_binning, false}, {"prefix          ", prefix, false},
+                        {"allocate        ", allocate, false}, {"numeric         ", numeric, false},
+                        {"cleanup         ", cleanup, false},  {"total           ", total, false}};
+    for (const Row &r : perf) std::printf("    %s %6.2lf\n", r.label, g / r.v);
 }
 
-void SpgemmTimings::reg_print(double total_flop) const { std::printf("%6.2lf\n", total > 0 ? total_flop / 1e9 / total : 0.0); }
+void SpgemmTimings::reg_print(double total_flop) const { std::printf("%6.2lf\n", total_flop / 1e9 / total); }
 
 void SpgemmTimings::perf_print(double total_flop) const
 {
     const double g = total_flop / 1e9;
-    std::printf("%6.2lf %6.2lf\n", symbolic > 0 ? g / symbolic : 0.0, numeric > 0 ? g / numeric : 0.0);
+    std::printf("%6.2lf %6.2lf\n", g / symbolic, g / numeric);
 }
 
 void SpgemmTimings::binning_print(double) const
 {
     const double b = symbolic_binning + numeric_binning;
-    std::printf("%.4le %.4lf\n", b, total > 0 ? 100 * b / total : 0.0);
+    std::printf("%.4le %.4lf\n", b, 100 * b / total);
 }
 
 const char *to_cstr(SpgemmStatus s)

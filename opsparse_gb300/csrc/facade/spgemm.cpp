@@ -163,4 +163,16 @@ SpgemmStatus opsparse_spgemm_safe(const CSR &A, const CSR &B, CSR &C, SpgemmMeta
     }
 }
 
+void opsparse_spgemm_backward(const CSR &A, const CSR &B, const CSR &C, const mdouble *d_dC, mdouble *d_dA,
+                              mdouble *d_dB, SpgemmMeta &meta)
+{
+    if (A.N != B.M) throw_on(OPS_NONSQUARE, nullptr);
+    if (C.M != A.M || C.N != B.N) throw std::runtime_error("opsparse_spgemm_backward: C is not A*B's shape");
+    ops_handle_s *h = meta.handle();
+    int s = ops_spgemm_backward(h, OPS_F64, A.M, A.N, B.N, A.d_rpt, A.d_col, A.d_val, A.nnz, B.d_rpt, B.d_col,
+                                B.d_val, B.nnz, C.d_rpt, C.d_col, d_dC, d_dA, d_dB, meta.stream);
+    if (s == OPS_OK) s = ops_spgemm_check(h, meta.stream);  // synchronizes the stream
+    throw_on(s, h);
+}
+
 }  // namespace opsparse

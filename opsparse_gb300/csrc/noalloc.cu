@@ -1,12 +1,13 @@
 // noalloc.cu — intermediate-product count that allocates no device memory.
 //
-// Some callers of this library cannot allocate device memory when they count products:
-// code that records a CUDA graph and must not insert allocation nodes into it, serving or
-// real-time loops that forbid the CUDA allocator after start-up (cudaMalloc can
-// synchronize the device and cudaMallocAsync changes pool state), and hosts that give
-// the library a fixed memory budget up front.  ops_flop (spgemm.cu) takes a small
-// device temporary from cudaMallocAsync on every call; ops_flop_noalloc below computes
-// the same result with its scratch in a file-scope __device__ array instead.
+// Some callers of this library cannot allocate device memory at the point where they count
+// products: serving or real-time loops that forbid the CUDA allocator once they are running
+// (cudaMalloc can synchronize the whole device, and cudaMallocAsync changes the state of a
+// memory pool another component may own), and hosts that hand the library a fixed memory
+// budget up front and account for every byte themselves.  ops_flop (spgemm.cu) takes a
+// small device temporary from cudaMallocAsync on every call; ops_flop_noalloc below
+// computes the same result with its scratch in a file-scope __device__ array instead, and
+// calls no allocating function (no cudaMalloc, cudaFree or allocating library routine).
 //
 // The scratch holds one 64-bit partial sum per CTA of the flop kernel, the total, a
 // completion ticket and an error flag: kNoAllocMaxBlocks partials cap the input at
@@ -15,11 +16,13 @@
 // process exits.
 //
 // Set-up: the first call on each device looks up the array's device address with
-// cudaGetSymbolAddress (with that device current) and caches it; make that first call
-// before any stream capture.  All calls share the one array and it keeps the previous
-// call's contents, so each call clears the words that must start at zero; calls whose
-// work overlaps on the GPU (two streams, or two host threads) race on it and must be
-// serialized by the caller.
+// cudaGetSymbolAddress (with that device current) and keeps it for later calls; make that
+// first call before any stream capture.  Like the library's handles, the kept address does
+// not survive cudaDeviceReset: do not call the library across a device reset.  All calls
+// share the one array and it keeps the previous call's contents, so each call clears the
+// words that must start at zero; calls whose work overlaps on the GPU (two streams, or two
+// host threads) race on it and must be serialized by the caller.  The call reads the total
+// back to the host and synchronizes its stream before it returns.
 #include <cstdint>
 #include <mutex>
 

@@ -30,10 +30,12 @@
  *    phases, per-thread open-addressing tables), the timed CPU baseline.  Same summation order as
  *    orc_spgemm_f64, so its output is bit-identical to it.
  *
- * Pinning: flop counts are checked against the reference's own host compute_flop
- * compiled from its sources (oracle/ref_host.mk); structure and values are checked
- * against an independent implementation (scipy.sparse) and against the known sizes of
- * the Laplacian and 27-point configurations.
+ * Pinning: flop counts, structure and values are checked against the reference's own
+ * kernels and host compute_flop, compiled from its sources and run on the CPU
+ * (oracle/ref_emul/, through the golden fixtures tests/golden/*.npz that
+ * tests/golden/make_golden.py made with them), and against the same kernels on the GPU
+ * (oracle/ref_gpu/); also against an independent implementation (scipy.sparse) and the
+ * known sizes of the Laplacian and 27-point configurations.
  *
  * Build: gcc -O2 -fopenmp -ffp-contract=off -shared -fPIC (oracle/Makefile).  Contraction
  * must stay off: every rounding step above is spelled out explicitly.

@@ -15,21 +15,36 @@ import numpy as np
 
 HERE = Path(__file__).resolve().parent
 SO = HERE / "_ref" / "libref_opsparse.so"
-SRC_DIR = Path(os.environ.get("OPSPARSE_SRC", "/root/reference"))
 _LIB = None
 
 
+def make_vars() -> list[str]:
+    """make variables naming the OpSparse source tree: OPSPARSE_SRC from the environment
+    when set, else none (the recipe's own default applies)."""
+    src = os.environ.get("OPSPARSE_SRC")
+    return [f"OPSPARSE_SRC={src}"] if src else []
+
+
+def has_sources(recipe_dir: Path) -> bool:
+    """Whether the recipe in `recipe_dir` finds the OpSparse source tree."""
+    try:
+        res = subprocess.run(["make", "-s", "-C", str(recipe_dir), *make_vars(), "has-src"],
+                             stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
+    except OSError:  # no make on this machine
+        return False
+    return res.returncode == 0
+
+
 def available() -> bool:
-    return SO.exists() or (SRC_DIR / "include" / "opsparse").is_dir()
+    return SO.exists() or has_sources(HERE / "ref_emul")
 
 
 def build(force: bool = False) -> Path:
     srcs = [HERE / "ref_emul" / f for f in ("ref_driver.cpp", "emul.cpp", "cuda_emul.hpp")]
     if force or not SO.exists() or any(SO.stat().st_mtime < s.stat().st_mtime for s in srcs):
-        if not (SRC_DIR / "include" / "opsparse").is_dir():
-            raise RuntimeError(f"OpSparse sources not found at {SRC_DIR}")
-        subprocess.run(["make", "-s", "-C", str(HERE / "ref_emul"), f"OPSPARSE_SRC={SRC_DIR}", f"OUT={SO.parent}"],
-                       check=True)
+        if not has_sources(HERE / "ref_emul"):
+            raise RuntimeError("OpSparse sources not found (set OPSPARSE_SRC to its source tree)")
+        subprocess.run(["make", "-s", "-C", str(HERE / "ref_emul"), *make_vars(), f"OUT={SO.parent}"], check=True)
     return SO
 
 

@@ -10,17 +10,17 @@ bench.py to time the reference with its own protocol (1 warm-up, mean of 10 call
 from __future__ import annotations
 
 import ctypes as C
-import os
 import shutil
 import subprocess
 from pathlib import Path
+
+from .ref import has_sources, make_vars
 
 HERE = Path(__file__).resolve().parent
 OUT = HERE / "_ref"
 CUBIN = OUT / "ref_kernels.cubin"
 NAMES = OUT / "ref_kernels.names"
 SO = OUT / "libref_gpu.so"
-SRC_DIR = Path(os.environ.get("OPSPARSE_SRC", "/root/reference"))
 _LIB = None
 
 
@@ -38,10 +38,10 @@ def build(force: bool = False) -> bool:
     if nvcc is None:
         return False
     kern = HERE / "ref_gpu" / "kernels.cu"
-    if (SRC_DIR / "include" / "opsparse").is_dir() and (
-            force or not CUBIN.exists() or CUBIN.stat().st_mtime < kern.stat().st_mtime):
-        subprocess.run(["make", "-s", "-C", str(HERE / "ref_gpu"), f"OPSPARSE_SRC={SRC_DIR}", f"OUT={OUT}",
-                        f"NVCC={nvcc}"], check=True)
+    if (force or not CUBIN.exists() or CUBIN.stat().st_mtime < kern.stat().st_mtime) and \
+            has_sources(HERE / "ref_gpu"):
+        subprocess.run(["make", "-s", "-C", str(HERE / "ref_gpu"), *make_vars(), f"OUT={OUT}", f"NVCC={nvcc}"],
+                       check=True)
     if not (CUBIN.exists() and NAMES.exists()):
         return False
     drv = HERE / "ref_gpu" / "ref_gpu.cu"

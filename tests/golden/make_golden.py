@@ -2,7 +2,8 @@
 OpSparse's own SpGEMM kernels (compiled from its sources and run on the CPU by
 oracle/ref_emul) and of its host compute_flop.
 
-Run in a checkout that has the OpSparse sources (OPSPARSE_SRC, default /root/reference):
+Run where the OpSparse source tree is (OPSPARSE_SRC=<dir>, or the default of
+oracle/ref_emul/Makefile):
     python tests/golden/make_golden.py
 Each fixture holds a_rpt/a_col/a_val, b_rpt/b_col/b_val, ncols, the reference's
 c_rpt/c_col/c_val, its per-row flop counts, and the bin histograms its binning kernels

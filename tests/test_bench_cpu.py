@@ -63,3 +63,19 @@ def test_zero_entries_must_stay_zero(ref):
     g[2][0] = 1e-30
     rep = bench.parity_report(g, o, "f64")
     assert rep["zeros_exact"] is False and not rep["within_tolerance"]
+
+
+def test_fp32_cancellation_is_judged_against_the_terms(ref):
+    """An FP32 entry whose terms cancel may differ from the FP64 oracle by far more than
+    1e-5 of its own size; it is judged relative to 2^-24 * sum|a*b| of its terms."""
+    o = (ref[0], ref[1], ref[2].copy())
+    o[2][5] = 3e-9                       # the oracle's value of a cancelling entry
+    scale = np.abs(o[2]) + 1.0           # sum of |a*b| of each entry's terms
+    g = (ref[0].astype(np.int32), ref[1], o[2].astype(np.float32))
+    g[2][5] = np.float32(3e-9 + 2e-13)  # 7e-5 of the entry, 3e-6 of its terms' resolution
+    rep = bench.parity_report(g, o, "f32", scale_fn=lambda: scale)
+    assert rep["max_rel_err"] > 1e-5                   # the plain relative bound would fail it
+    assert rep["max_rel_err_scaled"] <= 1e-5 and rep["within_tolerance"]
+    g[2][5] = np.float32(1.0)                          # a real error stays an error
+    rep = bench.parity_report(g, o, "f32", scale_fn=lambda: scale)
+    assert not rep["within_tolerance"]

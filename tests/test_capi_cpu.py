@@ -2,6 +2,7 @@
 GPU, and export every function that include/opsparse_gb300.h declares."""
 import ctypes
 import subprocess
+from pathlib import Path
 
 import pytest
 
@@ -62,18 +63,16 @@ def test_no_device_work_without_gpu(built):
 
 def test_reference_benchmark_drivers_compile_against_dropin(built, tmp_path):
     """OpSparse's own benchmark drivers (benchmarks/opsparse_profile.cu, opsparse_reg.cu)
-    compile and link unchanged against include/opsparse/ and libopsparse.so."""
-    import os
-    from pathlib import Path
+    compile and link unchanged against include/opsparse/ and libopsparse.so (recipe:
+    oracle/dropin_check/Makefile)."""
+    from oracle.ref import has_sources, make_vars
 
-    src = Path(os.environ.get("OPSPARSE_SRC", "/root/reference")) / "benchmarks"
-    if not (src / "opsparse_reg.cu").exists():
+    recipe = Path(__file__).resolve().parents[1] / "oracle" / "dropin_check"
+    if not has_sources(recipe):
         pytest.skip("OpSparse sources not present")
-    nvcc = built._nvcc()
+    res = subprocess.run(["make", "-s", "-C", str(recipe), *make_vars(), f"NVCC={built._nvcc()}",
+                          f"INCLUDE={built.INCLUDE}", f"LIBDIR={built.OUT}", f"OUT={tmp_path}"],
+                         capture_output=True, text=True)
+    assert res.returncode == 0, res.stdout + res.stderr
     for name in ("opsparse_profile", "opsparse_reg"):
-        out = tmp_path / name
-        res = subprocess.run([nvcc, "-std=c++17", f"-I{built.INCLUDE}", f"-I{src}", str(src / f"{name}.cu"), "-o",
-                              str(out), f"-L{built.OUT}", "-lopsparse", "-lopsparse_gb300",
-                              f"-Xlinker=-rpath={built.OUT}"], capture_output=True, text=True)
-        assert res.returncode == 0, res.stdout + res.stderr
-        assert out.exists()
+        assert (tmp_path / name).exists()

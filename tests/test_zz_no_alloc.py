@@ -1,17 +1,19 @@
 """ops_flop_noalloc — the product counter for callers that may not allocate device memory
-(graph capture without allocation nodes, allocator-free serving loops, fixed budgets).
+(serving loops that forbid the CUDA allocator once running, hosts with a fixed memory
+budget).
 
-Called through the C ABI twice in a row on the same inputs; each call's per-row counts
-and total must equal ops_flop's (integers: exact).  The second call checks that the
-shared scratch array is reset between calls.  This file is collected last so that a run
-stopping at the first failure has already run every other test; it also passes on its
-own in a fresh process.
+Called through the C ABI twice in a row on the same inputs; each call's per-row counts and
+total must equal ops_flop's and the oracle's (integers: exact).  The second call checks
+that the shared scratch array is cleared between calls.  This file is collected last so
+that a run stopping at the first failure has already run every other test; it also passes
+on its own in a fresh process.
 """
 import ctypes as C
 
 import numpy as np
 import pytest
 
+import oracle
 from opsparse_gb300 import capi, gen
 
 pytestmark = pytest.mark.gpu
@@ -33,8 +35,9 @@ def test_noalloc_matches_ops_flop_twice(cuda):
     ref_total = C.c_int64(0)
     assert lib.ops_flop(n, n, d_rpt.data_ptr(), d_col.data_ptr(), d_rpt.data_ptr(), ref_rows.data_ptr(),
                         C.byref(ref_total), stream) == capi.OPS_OK
-    expect_rows = ref_rows.cpu().numpy()
-    assert ref_total.value == int(gen.row_flop(rpt, col, rpt).sum())
+    orc_total, orc_rows = oracle.flop(rpt, col, rpt)
+    assert ref_total.value == orc_total
+    assert np.array_equal(ref_rows.cpu().numpy(), orc_rows)
 
     for _ in range(2):
         rows = torch.full((n,), -1, dtype=torch.int64, device="cuda")
@@ -42,8 +45,8 @@ def test_noalloc_matches_ops_flop_twice(cuda):
         st = lib.ops_flop_noalloc(n, n, d_rpt.data_ptr(), d_col.data_ptr(), d_rpt.data_ptr(), rows.data_ptr(),
                                   C.byref(total), stream)
         assert st == capi.OPS_OK, capi.status_string(st)
-        assert total.value == ref_total.value
-        assert np.array_equal(rows.cpu().numpy(), expect_rows)
+        assert total.value == ref_total.value == orc_total
+        assert np.array_equal(rows.cpu().numpy(), orc_rows)
 
 
 def test_noalloc_refuses_oversized_input(cuda):
