@@ -678,6 +678,7 @@ def measure_batched(args, local_rank, count, reps_loop, reps_batch, reps_replay,
         replay_ms = _timed(lambda: bt.execute(True), reps_replay, stream)
     bt.check()
     seg, flop, nnz = bt.info()
+    persistent, warp_rows, cta_rows = bt.queues()
     # measured error of a seeded sample of the batch's results
     par = {"problems_checked": 0, "structure_identical": True, "within_tolerance": True, "max_abs_err": 0.0,
            "max_rel_err_scaled": 0.0, "entries": 0, "values_bit_identical_to_fp32_oracle": True,
@@ -712,6 +713,9 @@ def measure_batched(args, local_rank, count, reps_loop, reps_batch, reps_replay,
                        "segments": seg, "data": "synthetic (device-generated Erdos-Renyi pairs)"},
             "batched": {"loop_ms": loop_ms, "batched_ms": full_ms, "speedup_vs_loop": loop_ms / full_ms,
                         "graph_replay_numeric_ms": replay_ms, "target_speedup": 3.0,
+                        "plan": ("one setup kernel, then one persistent kernel per row-size queue and phase over "
+                                 "every problem's rows" if persistent else "per segment"),
+                        "queue_rows": {"warp": warp_rows, "cta": cta_rows},
                         "reps": {"loop": reps_loop, "batched": reps_batch, "replay": reps_replay}},
             "parity": par}
 

@@ -100,6 +100,24 @@ int ops_handle_set_output_malloc(ops_handle_t handle, int use_cuda_malloc);
  * ops_spgemm_numeric always run two passes.  No OpSparse counterpart: its symbolic and
  * numeric kernels always run separately (core_algo/spgemm/spgemm.cu:16-62). */
 int ops_handle_set_one_pass(ops_handle_t handle, int mode);
+/* Every run-time choice of kernels and sizes, in one record: the autotuner's search space.
+ * No OpSparse counterpart: its bin ranges, table sizes and threads per row are compile-time
+ * constants (include/opsparse/utils/config.hpp:6-27, kernels/binning.cuh:21,105). */
+typedef struct {
+    int32_t thresholds[6];    /* row-class bounds, see ops_handle_set_thresholds */
+    int32_t hash_slots;       /* slots per output entry of the E1 warp-hash numeric table (2 or 4,
+                                 default 4) */
+    int32_t batch_persistent; /* batches: 1 (default) = one setup kernel and one persistent
+                                 kernel per row-size queue and phase over every problem's rows
+                                 (where every row has at most 4,096 products and 1,280 A
+                                 entries), 0 = per-segment pipeline */
+    int32_t batch_warp_max;   /* threads per row in the persistent batch kernels: rows of at most
+                                 this many products (128..512, default 512) get one warp
+                                 (register sort), larger rows a 128-thread CTA (up to 1,024
+                                 products) or a 256-thread CTA (up to 4,096) */
+} ops_tuning;
+int ops_handle_set_tuning(ops_handle_t handle, const ops_tuning *tuning);
+int ops_handle_get_tuning(ops_handle_t handle, ops_tuning *tuning);
 /* Upper bound in bytes for the one-pass staging area (default 2 GiB); a call whose staged
  * products need more runs two passes.  No OpSparse counterpart. */
 int ops_handle_set_stage_budget(ops_handle_t handle, size_t bytes);
@@ -189,13 +207,17 @@ typedef struct {
 typedef struct ops_batch_s *ops_batch_t;
 
 /* Plans a batch: per-problem product counts, grouping into segments whose products fit
- * int32, block-diagonal layout of each segment, one row classification per segment over
- * all its problems, symbolic phase, scan, and allocation of every C_b.  The items' value
+ * int32 and block-diagonal layout of each segment; then, where every row has at most
+ * 4,096 products and 1,280 A entries (and ops_tuning.batch_persistent is on), one setup
+ * kernel that puts every row of every problem into one of four row-size queues and one
+ * persistent kernel per queue that counts them all; otherwise a row classification and
+ * symbolic phase per segment.  Then each segment's scan and the allocation of every C_b.  The items' value
  * pointers are read by ops_batch_execute, which may be called repeatedly with new values
  * in the same arrays.  The handle's row-class thresholds are used.  Synchronizes. */
 int ops_batch_create(ops_handle_t handle, int dtype, int32_t count, const ops_batch_item *items, ops_batch_t *batch,
                      void *stream);
-/* Numeric phase of every problem.  use_graph = 1: the first call records the work on
+/* Numeric phase of every problem: the value gathers and one persistent kernel per queue
+ * (or the per-segment numeric phases).  use_graph = 1: the first call records the work on
  * `stream` (a created stream) as a CUDA graph and later calls replay it with a single
  * cudaGraphLaunch; use_graph = 0: plain launches.  Asynchronous. */
 int ops_batch_execute(ops_batch_t batch, int use_graph, void *stream);
@@ -205,6 +227,11 @@ int ops_batch_check(ops_batch_t batch, void *stream);
 int ops_batch_result(ops_batch_t batch, int32_t index, int32_t **c_rpt, int32_t **c_col, void **c_val,
                      int64_t *c_nnz);
 int ops_batch_info(ops_batch_t batch, int32_t *segments, int64_t *flop, int64_t *nnz);
+/* How the batch was planned: *persistent = 1 when one setup kernel and one persistent kernel
+ * per row-size queue and phase cover all its problems (ops_tuning.batch_persistent), with
+ * the rows its warp-per-row and CTA-per-row queues hold; 0 (queues 0) when it runs segment
+ * by segment.  Diagnostic. */
+int ops_batch_queues(ops_batch_t batch, int32_t *persistent, int64_t *warp_rows, int64_t *cta_rows);
 /* Releases the batch (synchronizes).  Its device memory returns to the handle's pool and
  * its per-segment handles to the handle, both reused by the handle's next batch; destroy
  * every batch before its handle. */

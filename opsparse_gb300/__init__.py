@@ -120,6 +120,19 @@ class Handle:
         """ops_spgemm in one pass: 0 off, 1 on for large inputs (default), 2 on at any size."""
         check(self.lib.ops_handle_set_one_pass(self.h, int(mode)), self.h)
 
+    def get_tuning(self) -> dict:
+        """Every run-time kernel and size choice of the handle (ops_tuning)."""
+        t = capi.Tuning()
+        check(self.lib.ops_handle_get_tuning(self.h, C.byref(t)), self.h)
+        return t.as_dict()
+
+    def set_tuning(self, **kw):
+        """Changes the named fields of the handle's ops_tuning (thresholds, hash_slots,
+        batch_persistent, batch_warp_max)."""
+        cur = self.get_tuning()
+        cur.update(kw)
+        check(self.lib.ops_handle_set_tuning(self.h, C.byref(capi.Tuning.from_dict(cur))), self.h)
+
     def set_stage_budget(self, nbytes: int):
         """Largest one-pass staging area; beyond it ops_spgemm runs two passes."""
         check(self.lib.ops_handle_set_stage_budget(self.h, int(nbytes)), self.h)
@@ -242,6 +255,12 @@ class Batch:
         seg, fl, nz = C.c_int32(0), C.c_int64(0), C.c_int64(0)
         check(self.lib.ops_batch_info(self.b, C.byref(seg), C.byref(fl), C.byref(nz)))
         return int(seg.value), int(fl.value), int(nz.value)
+
+    def queues(self):
+        """(persistent, warp-queue rows, CTA-queue rows) of the batch's plan."""
+        p, w, c = C.c_int32(0), C.c_int64(0), C.c_int64(0)
+        check(self.lib.ops_batch_queues(self.b, C.byref(p), C.byref(w), C.byref(c)))
+        return bool(p.value), int(w.value), int(c.value)
 
     def result(self, i: int):
         """(rpt, col, val) numpy copies of C_i."""

@@ -60,6 +60,19 @@ class Timings(C.Structure):
         return d
 
 
+class Tuning(C.Structure):
+    _fields_ = [("thresholds", I32 * 6), ("hash_slots", I32), ("batch_persistent", I32), ("batch_warp_max", I32)]
+
+    def as_dict(self) -> dict:
+        return {"thresholds": list(self.thresholds), "hash_slots": self.hash_slots,
+                "batch_persistent": self.batch_persistent, "batch_warp_max": self.batch_warp_max}
+
+    @classmethod
+    def from_dict(cls, d):
+        return cls((I32 * 6)(*[int(x) for x in d["thresholds"]]), int(d["hash_slots"]), int(d["batch_persistent"]),
+                   int(d["batch_warp_max"]))
+
+
 class BatchItem(C.Structure):
     _fields_ = [("rows", I32), ("cols_a", I32), ("cols_b", I32), ("a_nnz", I64), ("b_nnz", I64),
                 ("a_rpt", P), ("a_col", P), ("a_val", P), ("b_rpt", P), ("b_col", P), ("b_val", P)]
@@ -76,6 +89,8 @@ _SIGS = {
     "ops_handle_set_output_malloc": (C.c_int, [P, C.c_int]),
     "ops_handle_set_one_pass": (C.c_int, [P, C.c_int]),
     "ops_handle_set_stage_budget": (C.c_int, [P, C.c_size_t]),
+    "ops_handle_set_tuning": (C.c_int, [P, C.POINTER(Tuning)]),
+    "ops_handle_get_tuning": (C.c_int, [P, C.POINTER(Tuning)]),
     "ops_handle_set_thresholds": (C.c_int, [P, C.POINTER(I32), C.c_int]),
     "ops_handle_get_thresholds": (C.c_int, [P, C.POINTER(I32), C.c_int]),
     "ops_handle_last_error": (C.c_char_p, [P]),
@@ -96,6 +111,7 @@ _SIGS = {
     "ops_batch_check": (C.c_int, [P, P]),
     "ops_batch_result": (C.c_int, [P, I32, C.POINTER(P), C.POINTER(P), C.POINTER(P), C.POINTER(I64)]),
     "ops_batch_info": (C.c_int, [P, C.POINTER(I32), C.POINTER(I64), C.POINTER(I64)]),
+    "ops_batch_queues": (C.c_int, [P, C.POINTER(I32), C.POINTER(I64), C.POINTER(I64)]),
     "ops_batch_destroy": (C.c_int, [P]),
     "ops_autotune": (C.c_int, [P, C.c_int, I32, C.POINTER(BatchItem), C.c_int, C.POINTER(I32), C.POINTER(C.c_float), P]),
     "ops_tuning_store": (C.c_int, [C.c_char_p, C.c_char_p, C.POINTER(I32)]),

@@ -22,6 +22,9 @@
 #include <new>
 #include <vector>
 
+#include <cub/cub.cuh>
+
+#include "batch_rows.cuh"
 #include "common.cuh"
 #include "internal.hpp"
 
@@ -53,7 +56,9 @@ struct Segment {
     int *c_rpt = nullptr, *c_col = nullptr;
     void *c_val = nullptr;
     long long c_nnz = 0;
-    ops_handle_s *h = nullptr;  // per-segment plan (classes, workspace)
+    ops_handle_s *h = nullptr;  // per-segment plan (classes, workspace); the per-segment path only
+    int *row_flop = nullptr;    // persistent path: per-row products
+    DevInfo *info = nullptr;    // persistent path: error flags of the segment's rows
 };
 
 // The batch helpers walk flattened element spaces: a segment's A entries (or rows, or
@@ -167,6 +172,15 @@ __global__ void k_batch_gather_vals(const Item *__restrict__ items, int count, l
     }
 }
 
+// Last row pointers of a segment's A and B (their entry counts).
+__global__ void k_batch_last(int *a_last, int a_nnz, int *b_last, int b_nnz)
+{
+    if (threadIdx.x == 0) {
+        *a_last = a_nnz;
+        *b_last = b_nnz;
+    }
+}
+
 int flat_grid(long long total, int sms) { return (int)std::max<long long>(1, std::min<long long>((total + kFlatChunk - 1) / kFlatChunk, (long long)sms * 16)); }
 
 // Per-problem row_ptr rebased to start at 0, written to the result arena.
@@ -195,6 +209,22 @@ struct ops_batch_s {
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     cudaStream_t graph_stream = nullptr;
+    // persistent path (batch_rows.cuh): one setup kernel, and one kernel per row-size queue
+    // and phase, over every segment
+    bool persistent = false;
+    bool key64 = false;            // numeric sort keys need 64 bits (a segment has > 2^20 columns)
+    void *pmem = nullptr;          // queues, per-row products, segment arguments, scan scratch
+    opsg::BatchQueues *q = nullptr;
+    int *queues = nullptr;         // [kNumBatchQueues][total_rows] global row numbers
+    long long total_rows = 0;      // rows of every segment
+    int queue_rows[kNumBatchQueues] = {};  // rows in each queue
+    int grid[2][kNumBatchQueues] = {};     // [symbolic, numeric][queue] persistent grid sizes
+    int *d_base = nullptr;         // [nseg + 1] first global row of each segment
+    SpgemmArgs<double> *d_sym = nullptr;  // symbolic arguments per segment
+    void *d_num = nullptr;         // numeric arguments per segment (SpgemmArgs<T>)
+    long long *d_totals = nullptr;
+    void *cub_tmp = nullptr;
+    size_t cub_bytes = 0;
 };
 
 extern "C" int ops_spgemm_symbolic(ops_handle_t, int32_t, int32_t, int32_t, const int32_t *, const int32_t *, int64_t,
@@ -222,6 +252,7 @@ void batch_release(ops_batch_s *b)
         if (s.c_val) cudaFreeAsync(s.c_val, 0);
     }
     if (b->mem) cudaFreeAsync(b->mem, 0);
+    if (b->pmem) cudaFreeAsync(b->pmem, 0);
     if (b->d_items) cudaFreeAsync(b->d_items, 0);
     cudaStreamSynchronize(0);
     (void)cudaGetLastError();
@@ -234,6 +265,285 @@ size_t seg_bytes(const Segment &s, size_t vs)
            align_up(vs * (size_t)std::max(1LL, s.a_nnz), 256) + align_up(4 * ((size_t)s.K + 1), 256) +
            align_up(4 * (size_t)std::max(1LL, s.b_nnz), 256) + align_up(vs * (size_t)std::max(1LL, s.b_nnz), 256) +
            align_up(4 * ((size_t)s.M + 1), 256);
+}
+
+
+#define OPS_CHECK_B(expr)                  \
+    do {                                   \
+        int s_ = (expr);                   \
+        if (s_ != OPS_OK) return bail(s_); \
+    } while (0)
+
+// C of one segment from the pool, its rebased per-problem row pointers.
+int alloc_segment_c(ops_batch_s *b, ops_handle_s *h, Segment &s, size_t vs, cudaStream_t st)
+{
+    void *cc = nullptr, *cv = nullptr;
+    cudaError_t e = cudaMallocFromPoolAsync(&cc, 4 * (size_t)std::max<long long>(s.c_nnz, 1), h->pool, st);
+    if (e == cudaSuccess) e = cudaMallocFromPoolAsync(&cv, vs * (size_t)std::max<long long>(s.c_nnz, 1), h->pool, st);
+    if (e != cudaSuccess) {
+        if (cc) cudaFreeAsync(cc, st);
+        return fail(h, status_of(e), "allocating a segment's C");
+    }
+    s.c_col = static_cast<int *>(cc);
+    s.c_val = cv;
+    if (s.count > 0) {
+        k_batch_rebase<<<std::min(s.count, 65535), 256, 0, st>>>(b->d_items, s.first, s.count, s.c_rpt,
+                                                                b->c_rpt_arena);
+        OPS_CUDA(h, cudaGetLastError());
+    }
+    return OPS_OK;
+}
+
+// Per-segment path: every segment classified, counted and scanned by the single-product
+// pipeline on a handle of its own.
+int plan_segments(ops_batch_s *b, ops_handle_s *h, size_t vs, cudaStream_t st)
+{
+    for (Segment &s : b->segs) {
+        int stt = OPS_OK;
+        if (!h->spare.empty()) {
+            s.h = h->spare.back();
+            h->spare.pop_back();
+        } else {
+            stt = ops_handle_create(&s.h);
+        }
+        if (stt != OPS_OK) return fail(h, stt, "creating a segment handle");
+        s.h->th = h->th;
+        s.h->hash_slots = h->hash_slots;
+        int64_t nnz = 0;
+        stt = ops_spgemm_symbolic(s.h, s.M, s.K, s.N, s.a_rpt, s.a_col, s.a_nnz, s.b_rpt, s.b_col, s.b_nnz, s.c_rpt,
+                                  &nnz, st);
+        if (stt != OPS_OK) return fail(h, stt, std::string("segment symbolic: ") + s.h->last_error);
+        s.c_nnz = nnz;
+        b->nnz += nnz;
+        OPS_CHECK(alloc_segment_c(b, h, s, vs, st));
+    }
+    return OPS_OK;
+}
+
+template <typename KernelT>
+int occupancy_grid(ops_handle_s *h, KernelT kernel, int threads, size_t smem)
+{
+    int per_sm = 0;
+    if (cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem) != cudaSuccess) {
+        (void)cudaGetLastError();
+        per_sm = 1;
+    }
+    return std::max(1, per_sm) * h->num_sms;
+}
+
+// Arguments of one segment's product.
+template <typename T>
+SpgemmArgs<T> seg_args(const Segment &s)
+{
+    SpgemmArgs<T> g{};
+    g.arpt = s.a_rpt;
+    g.acol = s.a_col;
+    g.aval = static_cast<const T *>(s.a_val);
+    g.brpt = s.b_rpt;
+    g.bcol = s.b_col;
+    g.bval = static_cast<const T *>(s.b_val);
+    g.M = s.M;
+    g.K = s.K;
+    g.N = s.N;
+    g.row_flop = s.row_flop;
+    g.c_rpt = s.c_rpt;
+    g.c_col = s.c_col;
+    g.c_val = static_cast<T *>(s.c_val);
+    g.info = s.info;
+    g.soff = nullptr;
+    return g;
+}
+
+// The persistent kernel of queue c for one phase, on stream s.  Grid sizes are the
+// kernel's occupancy on every SM, computed on first use.
+template <typename KernelT, typename T>
+int launch_queue(ops_batch_s *b, int phase, int c, KernelT kernel, int threads, size_t smem, const SpgemmArgs<T> *args,
+                 cudaStream_t s)
+{
+    ops_handle_s *h = b->owner;
+    int &grid = b->grid[phase][c];
+    if (!grid) grid = occupancy_grid(h, kernel, threads, smem);
+    kernel<<<grid, threads, smem, s>>>(args, b->d_base, (int)b->segs.size(), b->queues + (size_t)c * b->total_rows,
+                                       &b->q->count[c], &b->q->cursor[phase][c]);
+    OPS_CUDA(h, cudaGetLastError());
+    return OPS_OK;
+}
+
+// One phase of the persistent path: the kernel of every non-empty queue, each on a stream
+// of its own forked from st and joined back into it, so the queues share the GPU and none
+// waits for the tail of another.
+template <typename LaunchOne>
+int fork_queues(ops_batch_s *b, cudaStream_t st, LaunchOne launch_one)
+{
+    ops_handle_s *h = b->owner;
+    static_assert(kNumBatchQueues <= kNumClasses, "one handle stream per queue");
+    OPS_CUDA(h, cudaEventRecord(h->ev_fork, st));
+    for (int c = 0; c < kNumBatchQueues; ++c) {
+        if (b->queue_rows[c] <= 0) continue;
+        cudaStream_t s = h->side[c];
+        OPS_CUDA(h, cudaStreamWaitEvent(s, h->ev_fork, 0));
+        OPS_CHECK(launch_one(c, s));
+        OPS_CUDA(h, cudaEventRecord(h->ev_join[c], s));
+        OPS_CUDA(h, cudaStreamWaitEvent(st, h->ev_join[c], 0));
+    }
+    return OPS_OK;
+}
+
+int launch_batch_symbolic(ops_batch_s *b, cudaStream_t st)
+{
+    const SpgemmArgs<double> *a = b->d_sym;
+    constexpr int W = kBatchCountThreads / 32;
+    return fork_queues(b, st, [&](int c, cudaStream_t s) {
+        switch (c) {
+            case kQ128:
+                return launch_queue(b, 0, c, k_batch_count_rows<2 * kBatchQ128>, kBatchCountThreads,
+                                    (size_t)W * 2 * kBatchQ128 * sizeof(int), a, s);
+            case kQWarp:
+                return launch_queue(b, 0, c, k_batch_count_rows<2 * kBatchWarpMax>, kBatchCountThreads,
+                                    (size_t)W * 2 * kBatchWarpMax * sizeof(int), a, s);
+            case kQE1:
+                return launch_queue(b, 0, c, k_batch_count_rows<2 * BescE1::kCap>, kBatchCountThreads,
+                                    (size_t)W * 2 * BescE1::kCap * sizeof(int), a, s);
+            default:
+                return launch_queue(b, 0, c, k_batch_cta_rows<BescMid, false, double, unsigned>, BescMid::kThreads,
+                                    BescMid::smem<false, unsigned>(), a, s);
+        }
+    });
+}
+
+template <typename T, typename KT>
+int launch_batch_numeric(ops_batch_s *b, cudaStream_t st)
+{
+    static_assert(sizeof(SpgemmArgs<T>) == sizeof(SpgemmArgs<double>), "argument layout is the value type's");
+    const SpgemmArgs<T> *a = static_cast<const SpgemmArgs<T> *>(b->d_num);
+    return fork_queues(b, st, [&](int c, cudaStream_t s) {
+        switch (c) {
+            case kQ128:
+                return launch_queue(b, 1, c, k_batch_warp_rows<4, T, KT>, WsortShape<4>::kThreads,
+                                    WsortShape<4>::smem<true, T, KT>(), a, s);
+            case kQWarp:
+                return launch_queue(b, 1, c, k_batch_warp_rows<16, T, KT>, WsortShape<16>::kThreads,
+                                    WsortShape<16>::smem<true, T, KT>(), a, s);
+            case kQE1:
+                return launch_queue(b, 1, c, k_batch_cta_rows<BescE1, true, T, KT>, BescE1::kThreads,
+                                    BescE1::smem<true, KT>(), a, s);
+            default:
+                return launch_queue(b, 1, c, k_batch_cta_rows<BescMid, true, T, KT>, BescMid::kThreads,
+                                    BescMid::smem<true, KT>(), a, s);
+        }
+    });
+}
+
+// Persistent path: when the batch has at most kBatchMaxSegs segments and every row fits one
+// of the queues (batch_rows.cuh), classifies every row of every segment with one kernel,
+// counts them with one persistent kernel per queue, scans each segment's row pointers and
+// allocates C.  Leaves `used` false, having changed nothing a per-segment plan needs, when
+// the batch does not qualify.
+int plan_persistent(ops_batch_s *b, ops_handle_s *h, size_t vs, cudaStream_t st, bool &used)
+{
+    used = false;
+    const int nseg = (int)b->segs.size();
+    if (!h->batch_persistent || nseg == 0 || nseg > kBatchMaxSegs) return OPS_OK;
+    long long total_rows = 0;
+    int max_m = 0, max_n = 0;
+    for (const Segment &s : b->segs) {
+        total_rows += s.M;
+        max_m = std::max(max_m, s.M);
+        max_n = std::max(max_n, s.N);
+    }
+    if (total_rows == 0 || total_rows > INT_MAX) return OPS_OK;
+    size_t cub_bytes = 0;
+    OPS_CUDA(h, cub::DeviceScan::ExclusiveSum(nullptr, cub_bytes, (int *)nullptr, (int *)nullptr, max_m + 1));
+    const size_t A = 256;
+    size_t bytes = align_up(sizeof(BatchQueues), A) + align_up(4 * (size_t)kNumBatchQueues * total_rows, A) +
+                   align_up(4 * (size_t)(nseg + 1), A) + 2 * align_up(sizeof(SpgemmArgs<double>) * nseg, A) +
+                   align_up(8 * (size_t)nseg, A) + align_up(cub_bytes, A) + align_up(sizeof(DevInfo) * nseg, A);
+    for (const Segment &s : b->segs) bytes += align_up(4 * (size_t)std::max(1, s.M), A);
+    void *pm = nullptr;
+    OPS_CUDA(h, cudaMallocFromPoolAsync(&pm, bytes, h->pool, st));
+    b->pmem = pm;
+    unsigned char *m = static_cast<unsigned char *>(pm);
+    auto carve = [&](size_t n) {
+        unsigned char *p = m;
+        m += align_up(n, A);
+        return p;
+    };
+    b->total_rows = total_rows;
+    b->q = reinterpret_cast<BatchQueues *>(carve(sizeof(BatchQueues)));
+    b->queues = reinterpret_cast<int *>(carve(4 * (size_t)kNumBatchQueues * total_rows));
+    b->d_base = reinterpret_cast<int *>(carve(4 * (size_t)(nseg + 1)));
+    b->d_sym = reinterpret_cast<SpgemmArgs<double> *>(carve(sizeof(SpgemmArgs<double>) * nseg));
+    b->d_num = carve(sizeof(SpgemmArgs<double>) * nseg);
+    b->d_totals = reinterpret_cast<long long *>(carve(8 * (size_t)nseg));
+    b->cub_tmp = carve(cub_bytes);
+    b->cub_bytes = cub_bytes;
+    DevInfo *infos = reinterpret_cast<DevInfo *>(carve(sizeof(DevInfo) * nseg));
+    std::vector<int> base(nseg + 1, 0);
+    std::vector<SpgemmArgs<double>> sym(nseg);
+    for (int i = 0; i < nseg; ++i) {
+        Segment &s = b->segs[i];
+        s.row_flop = reinterpret_cast<int *>(carve(4 * (size_t)std::max(1, s.M)));
+        s.info = infos + i;
+        base[i + 1] = base[i] + s.M;
+        sym[i] = seg_args<double>(s);
+    }
+    // pageable copies: the source is staged before the call returns
+    OPS_CUDA(h, cudaMemcpyAsync(b->d_base, base.data(), 4 * (size_t)(nseg + 1), cudaMemcpyHostToDevice, st));
+    OPS_CUDA(h, cudaMemcpyAsync(b->d_sym, sym.data(), sizeof(SpgemmArgs<double>) * nseg, cudaMemcpyHostToDevice, st));
+    OPS_CUDA(h, cudaMemsetAsync(b->q, 0, sizeof(BatchQueues), st));
+    OPS_CUDA(h, cudaMemsetAsync(infos, 0, sizeof(DevInfo) * nseg, st));
+    for (const Segment &s : b->segs) OPS_CUDA(h, cudaMemsetAsync(s.c_rpt + s.M, 0, sizeof(int), st));
+    const int warp_max = std::max(kBatchQ128, std::min(kBatchWarpMax, h->batch_warp_max));
+    k_batch_setup<<<(int)std::min<long long>((total_rows + 255) / 256, (long long)h->num_sms * 16), 256, 0, st>>>(
+        b->d_sym, b->d_base, nseg, (int)total_rows, warp_max, b->queues, b->q);
+    OPS_CUDA(h, cudaGetLastError());
+    BatchQueues hq{};
+    OPS_CUDA(h, cudaMemcpyAsync(&hq, b->q, sizeof(BatchQueues), cudaMemcpyDeviceToHost, st));
+    OPS_CUDA(h, cudaStreamSynchronize(st));
+    if (hq.flags & kErrBadColumn) return fail(h, OPS_INVALID_CSR, "A has a column index outside [0, cols)");
+    for (int c = 0; c < kNumBatchQueues; ++c) b->queue_rows[c] = hq.count[c];
+    if (hq.count[kQBeyond] > 0) {  // rows beyond the queues: the per-segment pipeline takes the batch
+        OPS_CUDA(h, cudaFreeAsync(pm, st));
+        b->pmem = nullptr;
+        for (Segment &s : b->segs) {
+            s.row_flop = nullptr;
+            s.info = nullptr;
+        }
+        return OPS_OK;
+    }
+    // symbolic: one persistent kernel per queue, then each segment's scan
+    OPS_CHECK(launch_batch_symbolic(b, st));
+    for (const Segment &s : b->segs) {
+        size_t cb = cub_bytes;
+        OPS_CUDA(h, cub::DeviceScan::ExclusiveSum(b->cub_tmp, cb, s.c_rpt, s.c_rpt, s.M + 1, st));
+    }
+    k_batch_totals<double><<<1, 64, 0, st>>>(b->d_sym, nseg, b->d_totals);
+    OPS_CUDA(h, cudaGetLastError());
+    std::vector<long long> totals(nseg);
+    std::vector<DevInfo> hinfo(nseg);
+    OPS_CUDA(h, cudaMemcpyAsync(totals.data(), b->d_totals, 8 * (size_t)nseg, cudaMemcpyDeviceToHost, st));
+    OPS_CUDA(h, cudaMemcpyAsync(hinfo.data(), infos, sizeof(DevInfo) * nseg, cudaMemcpyDeviceToHost, st));
+    OPS_CUDA(h, cudaStreamSynchronize(st));
+    for (int i = 0; i < nseg; ++i) {
+        if (hinfo[i].flags & kErrBadColumn) return fail(h, OPS_INVALID_CSR, "B has a column index outside [0, cols)");
+        if (hinfo[i].flags & kErrProbeLimit) return fail(h, OPS_PROBE_LIMIT, "symbolic hash table overflow");
+        if (totals[i] > INT_MAX || totals[i] < 0) return fail(h, OPS_INT32_OVERFLOW, "a segment's nnz exceeds INT32_MAX");
+    }
+    // C of every segment; numeric arguments
+    std::vector<SpgemmArgs<double>> num(nseg);
+    for (int i = 0; i < nseg; ++i) {
+        Segment &s = b->segs[i];
+        s.c_nnz = totals[i];
+        b->nnz += s.c_nnz;
+        OPS_CHECK(alloc_segment_c(b, h, s, vs, st));
+        num[i] = seg_args<double>(s);  // the value pointers are reinterpreted by the value type
+    }
+    OPS_CUDA(h, cudaMemcpyAsync(b->d_num, num.data(), sizeof(SpgemmArgs<double>) * nseg, cudaMemcpyHostToDevice, st));
+    b->key64 = max_n > (1 << (32 - BescMid::kIdBits));  // the widest product index of the numeric keys
+    b->persistent = true;
+    used = true;
+    return OPS_OK;
 }
 
 }  // namespace
@@ -378,10 +688,9 @@ extern "C" int ops_batch_create(ops_handle_t h, int dtype, int32_t count, const 
         m += align_up(vs * (size_t)std::max(1LL, s.b_nnz), 256);
         s.c_rpt = reinterpret_cast<int *>(m);
         m += align_up(4 * ((size_t)s.M + 1), 256);
-        // 3. structure, last row pointers, classification + symbolic + scan
-        const int last_a = (int)s.a_nnz, last_b = (int)s.b_nnz;
-        cudaError_t e = cudaMemcpyAsync(s.a_rpt + s.M, &last_a, sizeof(int), cudaMemcpyHostToDevice, st);
-        if (e == cudaSuccess) e = cudaMemcpyAsync(s.b_rpt + s.K, &last_b, sizeof(int), cudaMemcpyHostToDevice, st);
+        // 3. structure and last row pointers (no host sync)
+        k_batch_last<<<1, 32, 0, st>>>(s.a_rpt + s.M, (int)s.a_nnz, s.b_rpt + s.K, (int)s.b_nnz);
+        cudaError_t e = cudaGetLastError();
         if (e == cudaSuccess && s.count > 0) {
             const Item *its = b->d_items + s.first;
             const int sms = h->num_sms;
@@ -393,39 +702,14 @@ extern "C" int ops_batch_create(ops_handle_t h, int dtype, int32_t count, const 
                 k_batch_gather_field<kFBCol><<<flat_grid(s.b_nnz, sms), 256, 0, st>>>(its, s.count, s.b_nnz, s.b_col);
             e = cudaGetLastError();
         }
-        if (e == cudaSuccess) e = cudaStreamSynchronize(st);  // host values above must outlive the copies
         if (e != cudaSuccess) return bail(fail(h, status_of(e), std::string("batch gather: ") + cudaGetErrorString(e)));
-        int stt = OPS_OK;
-        if (!h->spare.empty()) {
-            s.h = h->spare.back();
-            h->spare.pop_back();
-        } else {
-            stt = ops_handle_create(&s.h);
-        }
-        if (stt != OPS_OK) return bail(fail(h, stt, "creating a segment handle"));
-        s.h->th = h->th;
-        int64_t nnz = 0;
-        stt = ops_spgemm_symbolic(s.h, s.M, s.K, s.N, s.a_rpt, s.a_col, s.a_nnz, s.b_rpt, s.b_col, s.b_nnz, s.c_rpt,
-                                  &nnz, st);
-        if (stt != OPS_OK) return bail(fail(h, stt, std::string("segment symbolic: ") + s.h->last_error));
-        s.c_nnz = nnz;
-        b->nnz += nnz;
-        void *cc = nullptr, *cv = nullptr;
-        e = cudaMallocFromPoolAsync(&cc, 4 * (size_t)std::max<int64_t>(nnz, 1), h->pool, st);
-        if (e == cudaSuccess) e = cudaMallocFromPoolAsync(&cv, vs * (size_t)std::max<int64_t>(nnz, 1), h->pool, st);
-        if (e != cudaSuccess) {
-            if (cc) cudaFreeAsync(cc, st);
-            return bail(fail(h, status_of(e), "allocating a segment's C"));
-        }
-        s.c_col = static_cast<int *>(cc);
-        s.c_val = cv;
-        if (s.count > 0) {
-            k_batch_rebase<<<std::min(s.count, 65535), 256, 0, st>>>(b->d_items, s.first, s.count, s.c_rpt,
-                                                                    b->c_rpt_arena);
-            e = cudaGetLastError();
-            if (e != cudaSuccess) return bail(fail(h, status_of(e), "rebasing row pointers"));
-        }
     }
+    // 4. classification, symbolic phase, scan and C: one setup kernel and one persistent
+    // kernel per row-size queue over every segment, or segment by segment when some row is
+    // beyond the queues
+    bool persistent = false;
+    OPS_CHECK_B(plan_persistent(b, h, vs, st, persistent));
+    if (!persistent) OPS_CHECK_B(plan_segments(b, h, vs, st));
     cudaError_t e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return bail(fail(h, status_of(e), "batch create"));
     *out = b;
@@ -434,7 +718,8 @@ extern "C" int ops_batch_create(ops_handle_t h, int dtype, int32_t count, const 
 
 namespace {
 
-int record_numeric(ops_batch_s *b, cudaStream_t st)
+// Values of every segment's A and B gathered from the problems' arrays.
+int gather_values(ops_batch_s *b, cudaStream_t st)
 {
     ops_handle_s *h = b->owner;
     for (Segment &s : b->segs) {
@@ -457,6 +742,26 @@ int record_numeric(ops_batch_s *b, cudaStream_t st)
                     its, s.count, s.b_nnz, static_cast<float *>(s.b_val));
         }
         OPS_CUDA(h, cudaGetLastError());
+    }
+    return OPS_OK;
+}
+
+int record_numeric(ops_batch_s *b, cudaStream_t st)
+{
+    ops_handle_s *h = b->owner;
+    OPS_CHECK(gather_values(b, st));
+    if (b->persistent) {
+        // cursors and flags of the numeric pass start at zero
+        OPS_CUDA(h, cudaMemsetAsync(b->q->cursor[1], 0, sizeof(b->q->cursor[1]), st));
+        OPS_CUDA(h, cudaMemsetAsync(b->segs[0].info, 0, sizeof(DevInfo) * b->segs.size(), st));
+        if (b->dtype == OPS_F64)
+            return b->key64 ? launch_batch_numeric<double, unsigned long long>(b, st)
+                            : launch_batch_numeric<double, unsigned>(b, st);
+        return b->key64 ? launch_batch_numeric<float, unsigned long long>(b, st)
+                        : launch_batch_numeric<float, unsigned>(b, st);
+    }
+    for (Segment &s : b->segs) {
+        if (s.count == 0) continue;
         const int stt = ops_spgemm_numeric(s.h, b->dtype, s.M, s.K, s.N, s.a_rpt, s.a_col, s.a_val, s.b_rpt, s.b_col,
                                            s.b_val, s.c_rpt, s.c_col, s.c_val, st);
         if (stt != OPS_OK) return fail(h, stt, std::string("segment numeric: ") + s.h->last_error);
@@ -507,6 +812,20 @@ extern "C" int ops_batch_execute(ops_batch_t b, int use_graph, void *stream)
 extern "C" int ops_batch_check(ops_batch_t b, void *stream)
 {
     if (!b) return OPS_INVALID_ARGUMENT;
+    if (b->persistent) {
+        std::vector<DevInfo> hinfo(b->segs.size());
+        cudaStream_t st = static_cast<cudaStream_t>(stream);
+        OPS_CUDA(b->owner, cudaMemcpyAsync(hinfo.data(), b->segs[0].info, sizeof(DevInfo) * hinfo.size(),
+                                           cudaMemcpyDeviceToHost, st));
+        OPS_CUDA(b->owner, cudaStreamSynchronize(st));
+        for (const DevInfo &d : hinfo) {
+            if (d.flags & kErrBadColumn) return fail(b->owner, OPS_INVALID_CSR, "B has a column index outside [0, cols)");
+            if (d.flags & kErrCountMismatch)
+                return fail(b->owner, OPS_COUNT_MISMATCH, "numeric found a different nnz than symbolic");
+            if (d.flags & kErrProbeLimit) return fail(b->owner, OPS_PROBE_LIMIT, "hash table overflow");
+        }
+        return OPS_OK;
+    }
     for (Segment &s : b->segs) {
         if (s.count == 0) continue;
         const int stt = ops_spgemm_check(s.h, stream);
@@ -541,6 +860,15 @@ extern "C" int ops_batch_info(ops_batch_t b, int32_t *segments, int64_t *flop, i
     if (segments) *segments = (int32_t)b->segs.size();
     if (flop) *flop = b->flop;
     if (nnz) *nnz = b->nnz;
+    return OPS_OK;
+}
+
+extern "C" int ops_batch_queues(ops_batch_t b, int32_t *persistent, int64_t *warp_rows, int64_t *cta_rows)
+{
+    if (!b || !persistent || !warp_rows || !cta_rows) return OPS_INVALID_ARGUMENT;
+    *persistent = b->persistent ? 1 : 0;
+    *warp_rows = b->persistent ? (int64_t)b->queue_rows[kQ128] + b->queue_rows[kQWarp] : 0;
+    *cta_rows = b->persistent ? (int64_t)b->queue_rows[kQE1] + b->queue_rows[kQMid] : 0;
     return OPS_OK;
 }
 

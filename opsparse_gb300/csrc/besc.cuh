@@ -197,106 +197,135 @@ __device__ __forceinline__ int besc_sort_fold(const SpgemmArgs<T> &g, int n, int
     return total;
 }
 
+// Shared memory of one CTA of the besc routine: [keys | ids + heads] [own] [scan].
+template <typename Shape, bool kNum, typename KT>
+struct BescSmem {
+    KT *skeys;
+    unsigned short *spid;
+    int *hidx;
+    unsigned short *own;
+    int *s_incl;
+    int *s_b0;
+    __device__ __forceinline__ explicit BescSmem(unsigned char *p)
+    {
+        skeys = reinterpret_cast<KT *>(p);
+        spid = reinterpret_cast<unsigned short *>(p);
+        hidx = reinterpret_cast<int *>(p + Shape::up16(2 * (size_t)Shape::kCap));
+        p += Shape::template region0<kNum, KT>();
+        own = nullptr;
+        if constexpr (kNum) {
+            own = reinterpret_cast<unsigned short *>(p);
+            p += Shape::up16(2 * (size_t)Shape::kCap);
+        }
+        s_incl = reinterpret_cast<int *>(p);
+        s_b0 = s_incl + Shape::kAEntries;
+    }
+};
+
+// One row r (at most Shape::kCap products, Shape::kAEntries A entries) by the whole CTA:
+// expand, sort, then count (symbolic) or fold and write (numeric).  Symbolic and one-pass
+// calls write the row's count to c_rpt[r]; the count is also added to nnz_acc (thread 0).
+// s_warp_sums (32 ints), s_last (32 keys) and s_bad are block-shared scratch; *s_bad must
+// be 0 on entry and is 0 again on return.  Every thread of the CTA calls it; it ends with
+// a barrier.
+template <typename Shape, bool kNum, typename T, typename KT>
+__device__ __forceinline__ void besc_row(const SpgemmArgs<T> &g, int r, const BescSmem<Shape, kNum, KT> &sm,
+                                         int *s_warp_sums, KT *s_last, unsigned *s_bad,
+                                         unsigned long long &nnz_acc)
+{
+    constexpr int NT = Shape::kThreads;
+    constexpr int kIdBits = kNum ? Shape::kIdBits : 0;
+    const int tid = threadIdx.x;
+    const int lane = lane_id();
+    const int warp = tid >> 5;
+    const int a0 = __ldg(g.arpt + r);
+    const int lenA = __ldg(g.arpt + r + 1) - a0;
+    const int n = esc_scan_row<NT, T>(g, a0, lenA, sm.s_incl, sm.s_b0, s_warp_sums);
+    int off = 0, n_expect = 0;
+    if constexpr (kNum) {
+        if (g.soff) {  // one-pass: the row's staging slot, count unknown
+            off = __ldg(g.soff + r);
+            n_expect = INT_MAX;
+        } else {
+            off = __ldg(g.c_rpt + r);
+            n_expect = __ldg(g.c_rpt + r + 1) - off;
+        }
+    }
+    // expansion: kUnroll chunks of 32 products per warp, loads in flight together
+    bool bad = false;
+    for (int c0 = warp * 32; c0 < n; c0 += kUnroll * NT) {
+        int oo[kUnroll], kk[kUnroll];
+        bool v[kUnroll];
+#pragma unroll
+        for (int u = 0; u < kUnroll; ++u) {
+            const int c = c0 + u * NT;
+            oo[u] = 0;
+            kk[u] = 0;
+            v[u] = c < n ? esc_expand_chunk(sm.s_incl, sm.s_b0, lenA, n, c, &oo[u], &kk[u]) : false;
+        }
+        int col[kUnroll];
+#pragma unroll
+        for (int u = 0; u < kUnroll; ++u) col[u] = v[u] ? __ldg(g.bcol + kk[u]) : 0;
+#pragma unroll
+        for (int u = 0; u < kUnroll; ++u) {
+            const int q = c0 + u * NT + lane;
+            if (!v[u] || q >= Shape::kCap) continue;  // listed rows have at most kCap products
+            bad |= (unsigned)col[u] >= (unsigned)g.N;
+            sm.skeys[bpad(q)] = ((KT)(unsigned)col[u] << kIdBits) | (KT)(kNum ? q : 0);
+            if constexpr (kNum) sm.own[q] = (unsigned short)oo[u];
+        }
+    }
+    if (bad) *s_bad = 1u;
+    __syncthreads();
+    if (tid == 0 && *s_bad) atomicOr(&g.info->flags, kErrBadColumn);
+    const int m = min(n, Shape::kCap);
+    constexpr int P = Shape::kPMax;
+    int total;
+    if (m <= NT * (P / 4)) {
+        total = besc_sort_fold<Shape, P / 4, kIdBits, kNum, T, KT>(g, m, a0, sm.skeys, sm.spid, sm.hidx, sm.own,
+                                                                   sm.s_incl, sm.s_b0, off, n_expect, s_warp_sums,
+                                                                   s_last);
+    } else if (m <= NT * (P / 2)) {
+        total = besc_sort_fold<Shape, P / 2, kIdBits, kNum, T, KT>(g, m, a0, sm.skeys, sm.spid, sm.hidx, sm.own,
+                                                                   sm.s_incl, sm.s_b0, off, n_expect, s_warp_sums,
+                                                                   s_last);
+    } else {
+        total = besc_sort_fold<Shape, P, kIdBits, kNum, T, KT>(g, m, a0, sm.skeys, sm.spid, sm.hidx, sm.own,
+                                                               sm.s_incl, sm.s_b0, off, n_expect, s_warp_sums,
+                                                               s_last);
+    }
+    if (!kNum || g.soff) {
+        if (tid == 0) {
+            g.c_rpt[r] = total;
+            nnz_acc += (unsigned long long)total;
+        }
+    }
+    __syncthreads();
+    if (tid == 0) *s_bad = 0u;  // read by every thread before the barrier above
+}
+
 template <typename Shape, bool kNum, typename T, typename KT>
 __global__ void __launch_bounds__(Shape::kThreads, Shape::kMinBlocks) k_besc_rows(SpgemmArgs<T> g, const int *__restrict__ list,
                                                                const int *count_ptr, int *cursor)
 {
-    constexpr int NT = Shape::kThreads;
-    constexpr int kIdBits = kNum ? Shape::kIdBits : 0;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int tid = threadIdx.x;
-    const int lane = lane_id();
-    const int warp = tid >> 5;
     __shared__ int s_warp_sums[32];
     __shared__ KT s_last[32];
     __shared__ int s_row;
     __shared__ unsigned s_bad;
-
-    unsigned char *p = smem_raw;
-    KT *skeys = reinterpret_cast<KT *>(p);
-    unsigned short *spid = reinterpret_cast<unsigned short *>(p);
-    int *hidx = reinterpret_cast<int *>(p + Shape::up16(2 * (size_t)Shape::kCap));
-    p += Shape::template region0<kNum, KT>();
-    unsigned short *own = nullptr;
-    if constexpr (kNum) {
-        own = reinterpret_cast<unsigned short *>(p);
-        p += Shape::up16(2 * (size_t)Shape::kCap);
-    }
-    int *s_incl = reinterpret_cast<int *>(p);
-    int *s_b0 = s_incl + Shape::kAEntries;
+    const BescSmem<Shape, kNum, KT> sm(smem_raw);
 
     const int count = *count_ptr;
     unsigned long long nnz_acc = 0;
+    if (tid == 0) s_bad = 0u;
     for (;;) {
-        if (tid == 0) {
-            s_row = atomicAdd(cursor, 1);
-            s_bad = 0;
-        }
+        if (tid == 0) s_row = atomicAdd(cursor, 1);
         __syncthreads();
         const int it = s_row;
         __syncthreads();
         if (it >= count) break;
-        const int r = __ldg(list + it);
-        const int a0 = __ldg(g.arpt + r);
-        const int lenA = __ldg(g.arpt + r + 1) - a0;
-        const int n = esc_scan_row<NT, T>(g, a0, lenA, s_incl, s_b0, s_warp_sums);
-        int off = 0, n_expect = 0;
-        if constexpr (kNum) {
-            if (g.soff) {  // one-pass: the row's staging slot, count unknown
-                off = __ldg(g.soff + r);
-                n_expect = INT_MAX;
-            } else {
-                off = __ldg(g.c_rpt + r);
-                n_expect = __ldg(g.c_rpt + r + 1) - off;
-            }
-        }
-        // expansion: kUnroll chunks of 32 products per warp, loads in flight together
-        bool bad = false;
-        for (int c0 = warp * 32; c0 < n; c0 += kUnroll * NT) {
-            int oo[kUnroll], kk[kUnroll];
-            bool v[kUnroll];
-#pragma unroll
-            for (int u = 0; u < kUnroll; ++u) {
-                const int c = c0 + u * NT;
-                oo[u] = 0;
-                kk[u] = 0;
-                v[u] = c < n ? esc_expand_chunk(s_incl, s_b0, lenA, n, c, &oo[u], &kk[u]) : false;
-            }
-            int col[kUnroll];
-#pragma unroll
-            for (int u = 0; u < kUnroll; ++u) col[u] = v[u] ? __ldg(g.bcol + kk[u]) : 0;
-#pragma unroll
-            for (int u = 0; u < kUnroll; ++u) {
-                const int q = c0 + u * NT + lane;
-                if (!v[u] || q >= Shape::kCap) continue;  // listed rows have at most kCap products
-                bad |= (unsigned)col[u] >= (unsigned)g.N;
-                skeys[bpad(q)] = ((KT)(unsigned)col[u] << kIdBits) | (KT)(kNum ? q : 0);
-                if constexpr (kNum) own[q] = (unsigned short)oo[u];
-            }
-        }
-        if (bad) s_bad = 1u;
-        __syncthreads();
-        if (tid == 0 && s_bad) atomicOr(&g.info->flags, kErrBadColumn);
-        const int m = min(n, Shape::kCap);
-        constexpr int P = Shape::kPMax;
-        int total;
-        if (m <= NT * (P / 4)) {
-            total = besc_sort_fold<Shape, P / 4, kIdBits, kNum, T, KT>(g, m, a0, skeys, spid, hidx, own, s_incl,
-                                                                       s_b0, off, n_expect, s_warp_sums, s_last);
-        } else if (m <= NT * (P / 2)) {
-            total = besc_sort_fold<Shape, P / 2, kIdBits, kNum, T, KT>(g, m, a0, skeys, spid, hidx, own, s_incl,
-                                                                       s_b0, off, n_expect, s_warp_sums, s_last);
-        } else {
-            total = besc_sort_fold<Shape, P, kIdBits, kNum, T, KT>(g, m, a0, skeys, spid, hidx, own, s_incl, s_b0,
-                                                                   off, n_expect, s_warp_sums, s_last);
-        }
-        if (!kNum || g.soff) {
-            if (tid == 0) {
-                g.c_rpt[r] = total;
-                nnz_acc += (unsigned long long)total;
-            }
-        }
-        __syncthreads();
+        besc_row<Shape, kNum, T, KT>(g, __ldg(list + it), sm, s_warp_sums, s_last, &s_bad, nnz_acc);
     }
     if (tid == 0 && nnz_acc) atomicAdd(&g.info->total_nnz, nnz_acc);
 }

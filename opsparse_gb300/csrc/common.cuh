@@ -122,6 +122,9 @@ struct SpgemmArgs {
     // the count to info->total_nnz, as the counting kernels do; k_place_staged moves the
     // entries into C after the scan.
     const int *soff;
+    // Slots per output entry of the warp-hash numeric table (2 or 4; 0 means 4), capped by
+    // the kernel's table capacity: a tuning knob of the E1 rows with few outputs.
+    int hash_slots;
 };
 
 __device__ __forceinline__ int lane_id() { return threadIdx.x & 31; }

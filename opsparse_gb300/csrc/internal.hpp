@@ -102,6 +102,13 @@ struct ops_handle_s {
     long long plan_d_flop = 0;    // products of the D rows
     long long plan_d_len_a = 0;   // A entries of the D rows
 
+    // batches: 1 = one setup kernel and one persistent kernel per row-size queue and phase,
+    // over every problem's rows (batch_rows.cuh), where every row fits the queues; 0 =
+    // per-segment pipeline.  batch_warp_max = the largest row (products) a warp takes.
+    int batch_persistent = 1;
+    int batch_warp_max = 512;
+    int hash_slots = 4;  // slots per output entry of the E1 warp-hash numeric table (2 or 4)
+
     size_t map_budget = size_t(8) << 30;  // largest product map the backward may keep
     opsg::Thresholds th = opsg::default_thresholds();
     opsg::Thresholds plan_th = opsg::default_thresholds();  // thresholds the current plan was built with

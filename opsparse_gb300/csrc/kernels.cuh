@@ -558,7 +558,7 @@ __global__ void __launch_bounds__(256) k_reg_rows(SpgemmArgs<T> g, const int *__
 
 // Takes a class list's rows out of a one-pass call's staging (their staged product counts
 // to zero, before the counts are scanned into offsets).
-__global__ void k_unstage_rows(const int *__restrict__ list, const int *count_ptr, int *soff)
+static __global__ void k_unstage_rows(const int *__restrict__ list, const int *count_ptr, int *soff)
 {
     const int count = *count_ptr;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) soff[list[i]] = 0;
@@ -933,9 +933,10 @@ __global__ void __launch_bounds__(kWarpRowsThreads) k_warp_rows(SpgemmArgs<T> g,
         } else {
             n_expect = __ldg(g.row_flop + r);
         }
-        // numeric knows the row's output count: 4 slots per output where the table has
-        // room (fewer probe collisions), at least 2
-        const int log_ts = kNum ? min(ceil_log2_c(TMAX), max(5, ceil_log2(4 * max(n_expect, 1))))
+        // numeric knows the row's output count: hash_slots (default 4) slots per output
+        // where the table has room (fewer probe collisions), at least 2
+        const int log_ts = kNum ? min(ceil_log2_c(TMAX), max(5, ceil_log2((g.hash_slots ? g.hash_slots : 4) *
+                                                                           max(n_expect, 1))))
                                 : max(5, ceil_log2(2 * max(n_expect, 1)));
         const int row_products = kNum ? __ldg(g.row_flop + r) : n_expect;
         const bool rowwise = row_products >= 16 * (a1 - a0);

@@ -32,7 +32,9 @@ using namespace opsg_internal;
 
 namespace {
 
-const char *kVersion = "opsparse_gb300 0.1 (sm_103a)";
+const char *kVersion = "opsparse_gb300 0.2 (sm_103a)";
+constexpr int kBatchWarpMaxLo = 128;   // range of ops_tuning.batch_warp_max
+constexpr int kBatchWarpMaxHi = 512;
 
 struct Mat {
     int rows, cols;
@@ -714,6 +716,7 @@ int run_numeric(ops_handle_s *h, const Mat &A, const Mat &B, const int *c_rpt, i
     g.c_col = c_col;
     g.c_val = c_val;
     g.info = h->info;
+    g.hash_slots = h->hash_slots;
     return launch_classes<true, T>(h, g, st);
 }
 
@@ -930,6 +933,29 @@ int ops_handle_set_one_pass(ops_handle_t h, int mode)
 {
     if (!h || mode < 0 || mode > 2) return OPS_INVALID_ARGUMENT;
     h->one_pass = mode;
+    return OPS_OK;
+}
+
+int ops_handle_set_tuning(ops_handle_t h, const ops_tuning *t)
+{
+    if (!h || !t) return OPS_INVALID_ARGUMENT;
+    if ((t->hash_slots != 2 && t->hash_slots != 4) || (t->batch_persistent != 0 && t->batch_persistent != 1) ||
+        t->batch_warp_max < kBatchWarpMaxLo || t->batch_warp_max > kBatchWarpMaxHi)
+        return fail(h, OPS_INVALID_ARGUMENT, "tuning value out of range");
+    OPS_CHECK(ops_handle_set_thresholds(h, t->thresholds, 6));
+    h->hash_slots = t->hash_slots;
+    h->batch_persistent = t->batch_persistent;
+    h->batch_warp_max = t->batch_warp_max;
+    return OPS_OK;
+}
+
+int ops_handle_get_tuning(ops_handle_t h, ops_tuning *t)
+{
+    if (!h || !t) return OPS_INVALID_ARGUMENT;
+    OPS_CHECK(ops_handle_get_thresholds(h, t->thresholds, 6));
+    t->hash_slots = h->hash_slots;
+    t->batch_persistent = h->batch_persistent;
+    t->batch_warp_max = h->batch_warp_max;
     return OPS_OK;
 }
 
