@@ -405,9 +405,9 @@ int launch_batch_symbolic(ops_batch_s *b, cudaStream_t st)
             case kQE1:
                 return launch_queue(b, 0, c, k_batch_count_rows<2 * BescE1::kCap>, kBatchCountThreads,
                                     (size_t)W * 2 * BescE1::kCap * sizeof(int), a, s);
-            default:
-                return launch_queue(b, 0, c, k_batch_cta_rows<BescMid, false, double, unsigned>, BescMid::kThreads,
-                                    BescMid::smem<false, unsigned>(), a, s);
+            default:  // the table and the A-entry scan of EscMid's symbolic shape
+                return launch_queue(b, 0, c, k_batch_cta_count, EscMid::kThreads,
+                                    (size_t)EscMid::kTable * 4 + (size_t)EscMid::kAEntries * 8, a, s);
         }
     });
 }

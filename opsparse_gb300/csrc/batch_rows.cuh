@@ -14,7 +14,7 @@
 // empty, with the shape and occupancy of its row size:
 //   symbolic  kQ128, kQWarp, kQE1: a warp per row, distinct columns counted in a shared-memory
 //             hash table of 2 slots per product (256, 1,024, 2,048 slots);
-//             kQMid: a 256-thread CTA per row, expand / bitonic sort / count (besc.cuh);
+//             kQMid: a 256-thread CTA per row, hash table of 2 slots per product (esc.cuh);
 //   numeric   kQ128: a warp per row, register bitonic network of up to 128 keys, 8 warps per
 //             CTA (wsort.cuh); kQWarp: the same with networks of up to 512 keys, 4 warps per
 //             CTA; kQE1: a 128-thread CTA per row (besc.cuh, 1,024 keys); kQMid: a 256-thread
@@ -39,6 +39,7 @@ constexpr int kBatchChunk = 8;        // warp-queue rows a warp takes per cursor
 constexpr int kBatchMaxSegs = 16;     // segments one persistent launch covers (their arguments sit in shared memory)
 constexpr int kBatchCountThreads = 256;
 static_assert(WsortShape<4>::kMax == kBatchQ128 && WsortShape<16>::kMax == kBatchWarpMax, "warp-queue capacities");
+static_assert(EscMid::kProducts >= BescMid::kCap && EscMid::kAEntries >= BescMid::kAEntries, "kQMid rows fit both shapes");
 
 enum BatchQueue : int { kQ128 = 0, kQWarp = 1, kQE1 = 2, kQMid = 3, kQBeyond = 4, kNumBatchQueues = 4 };
 
@@ -186,19 +187,25 @@ __device__ __forceinline__ int warp_hash_count(const SpgemmArgs<double> &g, int 
 }
 
 // Symbolic persistent kernel of a warp queue (rows of at most TMAX/2 products): every warp
-// counts kBatchChunk rows per cursor step in its own table of at most TMAX slots.
+// counts kBatchChunk rows per cursor step in its own table of at most TMAX slots.  Rows of
+// at most 32 A entries whose B rows are long (16 or more products per A entry) and whose
+// products fall within kWinBits consecutive columns are counted over a window bitmap in
+// the same space instead (window_row_short, kernels.cuh), when it is large enough.
 template <int TMAX>
 __global__ void __launch_bounds__(kBatchCountThreads) k_batch_count_rows(const SpgemmArgs<double> *__restrict__ segs,
                                                                          const int *__restrict__ seg_row_base,
                                                                          int nseg, const int *__restrict__ queue,
                                                                          const int *count, int *cursor)
 {
+    constexpr bool kWindow = TMAX >= kWinWords;  // the table's space holds the window bitmap
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ SpgemmArgs<double> s_segs[kBatchMaxSegs];
     __shared__ int s_base[kBatchMaxSegs + 1];
     batch_load_segs<double>(segs, seg_row_base, nseg, s_segs, s_base);
     const int lane = lane_id();
     int *keys = reinterpret_cast<int *>(smem_raw) + (threadIdx.x >> 5) * TMAX;
+    bool win_clean = false;  // the window bitmap is all-zero
+    unsigned long long nnz_unused = 0;
     const int n = *count;
     for (;;) {
         int u0 = 0;
@@ -211,9 +218,18 @@ __global__ void __launch_bounds__(kBatchCountThreads) k_batch_count_rows(const S
             const int s = batch_segment(s_base, nseg, gr);
             const SpgemmArgs<double> &g = s_segs[s];
             const int r = gr - s_base[s];
+            const int a0 = __ldg(g.arpt + r), a1 = __ldg(g.arpt + r + 1);
             const int flop = __ldg(g.row_flop + r);
+            if (kWindow && flop >= 16 * (a1 - a0) && a1 - a0 <= 32) {
+                const int nnz_b = __ldg(g.brpt + g.K);
+                const bool bcol16 = ((size_t)g.bcol & 15) == 0;
+                if (window_row_short<double>(g, r, a0, a1, nnz_b, bcol16, reinterpret_cast<unsigned *>(keys),
+                                             win_clean, nnz_unused))
+                    continue;
+            }
+            win_clean = false;  // the hash table reuses the space
             const int log_ts = min(ceil_log2_c(TMAX), max(5, ceil_log2(2 * max(flop, 1))));
-            const int tot = warp_hash_count(g, __ldg(g.arpt + r), __ldg(g.arpt + r + 1), keys, log_ts);
+            const int tot = warp_hash_count(g, a0, a1, keys, log_ts);
             if (lane == 0) g.c_rpt[r] = tot;
             __syncwarp();
         }
@@ -280,6 +296,43 @@ __global__ void __launch_bounds__(Shape::kThreads, Shape::kMinBlocks)
         const int gr = __ldg(queue + u);
         const int s = batch_segment(s_base, nseg, gr);
         besc_row<Shape, kNum, T, KT>(s_segs[s], gr - s_base[s], sm, s_warp_sums, s_last, &s_bad, nnz_unused);
+    }
+}
+
+// Symbolic persistent kernel of the kQMid queue: every CTA counts one row per cursor step
+// in a shared-memory hash table (EscMid's symbolic shape).
+static __global__ void __launch_bounds__(EscMid::kThreads, 1) k_batch_cta_count(const SpgemmArgs<double> *__restrict__ segs,
+                                                                        const int *__restrict__ seg_row_base,
+                                                                        int nseg, const int *__restrict__ queue,
+                                                                        const int *count, int *cursor)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ SpgemmArgs<double> s_segs[kBatchMaxSegs];
+    __shared__ int s_base[kBatchMaxSegs + 1];
+    __shared__ int s_warp_sums[32];
+    __shared__ int s_unit;
+    __shared__ int s_count;
+    batch_load_segs<double>(segs, seg_row_base, nseg, s_segs, s_base);
+    int *table = reinterpret_cast<int *>(smem_raw);
+    int *s_incl = table + EscMid::kTable;
+    int *s_b0 = s_incl + EscMid::kAEntries;
+    const int n = *count;
+    for (;;) {
+        if (threadIdx.x == 0) s_unit = atomicAdd(cursor, 1);
+        __syncthreads();
+        const int u = s_unit;
+        __syncthreads();
+        if (u >= n) break;
+        const int gr = __ldg(queue + u);
+        const int s = batch_segment(s_base, nseg, gr);
+        const SpgemmArgs<double> &g = s_segs[s];
+        const int r = gr - s_base[s];
+        const int a0 = __ldg(g.arpt + r);
+        const int lenA = __ldg(g.arpt + r + 1) - a0;
+        const int flop = esc_scan_row<EscMid::kThreads, double>(g, a0, lenA, s_incl, s_b0, s_warp_sums);
+        const int tot = esc_count_row<EscMid, double>(g, lenA, flop, table, s_incl, s_b0, &s_count);
+        if (threadIdx.x == 0) g.c_rpt[r] = tot;
+        __syncthreads();
     }
 }
 

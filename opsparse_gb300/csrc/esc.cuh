@@ -142,6 +142,56 @@ __device__ __forceinline__ int esc_scan_row(const SpgemmArgs<T> &g, int a0, int 
     return running;
 }
 
+// Distinct columns of one row (lenA A entries already scanned into s_incl / s_b0, flop
+// products) by the whole CTA in a shared-memory hash table of at least 2 slots per product
+// (order-free claims; kUnroll chunks of column loads in flight before the first claim).
+// Returns the count on every thread; s_count is block-shared scratch.  Every thread of the
+// CTA calls it.
+template <typename Shape, typename T>
+__device__ __forceinline__ int esc_count_row(const SpgemmArgs<T> &g, int lenA, int flop, int *table,
+                                             const int *s_incl, const int *s_b0, int *s_count)
+{
+    constexpr int NT = Shape::kThreads;
+    const int tid = threadIdx.x;
+    const int lane = lane_id();
+    const int warp = tid >> 5;
+    const int log_ts = max(6, ceil_log2(2 * max(flop, 1)));
+    const int ts = 1 << log_ts;
+    for (int i = tid; i < ts; i += NT) table[i] = kEmpty;
+    if (tid == 0) *s_count = 0;
+    __syncthreads();
+    int cnt = 0;
+    for (int c0 = warp * 32; c0 < flop; c0 += kUnroll * NT) {
+        int kk[kUnroll];
+        bool v[kUnroll];
+#pragma unroll
+        for (int u = 0; u < kUnroll; ++u) {
+            const int c = c0 + u * NT;
+            int o = 0;
+            kk[u] = 0;
+            v[u] = c < flop ? esc_expand_chunk(s_incl, s_b0, lenA, flop, c, &o, &kk[u]) : false;
+        }
+        int col[kUnroll];
+#pragma unroll
+        for (int u = 0; u < kUnroll; ++u) col[u] = v[u] ? __ldg(g.bcol + kk[u]) : 0;
+#pragma unroll
+        for (int u = 0; u < kUnroll; ++u) {
+            if (!v[u]) continue;
+            if ((unsigned)col[u] >= (unsigned)g.N) {
+                atomicOr(&g.info->flags, kErrBadColumn);
+                continue;
+            }
+            bool is_new = false;
+            table_claim(table, col[u], log_ts, &is_new, &g.info->flags);
+            cnt += is_new ? 1 : 0;
+        }
+    }
+    cnt = (int)__reduce_add_sync(kFull, (unsigned)cnt);
+    if (lane == 0 && cnt) atomicAdd(s_count, cnt);
+    __syncthreads();
+    return *s_count;
+}
+
 template <typename Shape, bool kNum, typename T>
 __global__ void __launch_bounds__(Shape::kThreads, 1) k_esc_rows(SpgemmArgs<T> g, const int *__restrict__ list,
                                                               const int *count_ptr, int *cursor)
@@ -208,45 +258,10 @@ __global__ void __launch_bounds__(Shape::kThreads, 1) k_esc_rows(SpgemmArgs<T> g
 
         if constexpr (!kNum) {
             // ---------------------------------------------------------- symbolic --
-            const int log_ts = max(6, ceil_log2(2 * max(flop, 1)));
-            const int ts = 1 << log_ts;
-            for (int i = tid; i < ts; i += NT) table[i] = kEmpty;
-            if (tid == 0) s_count = 0;
-            __syncthreads();
-            int cnt = 0;
-            // kUnroll chunks per round: their column loads are all in flight before the
-            // first claim
-            for (int c0 = warp * 32; c0 < flop; c0 += kUnroll * NT) {
-                int kk[kUnroll];
-                bool v[kUnroll];
-#pragma unroll
-                for (int u = 0; u < kUnroll; ++u) {
-                    const int c = c0 + u * NT;
-                    int o = 0;
-                    kk[u] = 0;
-                    v[u] = c < flop ? esc_expand_chunk(s_incl, s_b0, lenA, flop, c, &o, &kk[u]) : false;
-                }
-                int col[kUnroll];
-#pragma unroll
-                for (int u = 0; u < kUnroll; ++u) col[u] = v[u] ? __ldg(g.bcol + kk[u]) : 0;
-#pragma unroll
-                for (int u = 0; u < kUnroll; ++u) {
-                    if (!v[u]) continue;
-                    if ((unsigned)col[u] >= (unsigned)g.N) {
-                        atomicOr(&g.info->flags, kErrBadColumn);
-                        continue;
-                    }
-                    bool is_new = false;
-                    table_claim(table, col[u], log_ts, &is_new, &g.info->flags);
-                    cnt += is_new ? 1 : 0;
-                }
-            }
-            cnt = (int)__reduce_add_sync(kFull, (unsigned)cnt);
-            if (lane == 0 && cnt) atomicAdd(&s_count, cnt);
-            __syncthreads();
+            const int tot = esc_count_row<Shape, T>(g, lenA, flop, table, s_incl, s_b0, &s_count);
             if (tid == 0) {
-                g.c_rpt[r] = s_count;
-                nnz_acc += (unsigned long long)s_count;
+                g.c_rpt[r] = tot;
+                nnz_acc += (unsigned long long)tot;
             }
             __syncthreads();
         } else {
