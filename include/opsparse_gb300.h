@@ -238,16 +238,25 @@ int ops_batch_queues(ops_batch_t batch, int32_t *persistent, int64_t *warp_rows,
 int ops_batch_destroy(ops_batch_t batch);
 
 /* ----------------------------------------------------------------- autotuner -- */
-/* Chooses the row-class thresholds (see ops_handle_set_thresholds) for a workload by
- * coordinate descent, timing complete batched runs of `items` (a representative sample)
- * with CUDA events, median of `reps` runs per candidate.  Installs the best thresholds on
- * the handle and returns them in best[6] (and the time in *best_ms).  Synchronizes. */
+/* Chooses every field of ops_tuning for a workload by coordinate descent: the row-class
+ * thresholds, the warp-hash table's slots per output entry (hash-table size), the batch
+ * plan (persistent kernels over row-size queues, or per segment) and the largest row a warp
+ * takes in the persistent kernels (threads per row: a warp, or a 128- or 256-thread CTA
+ * above it).  Each candidate is timed as complete batched runs of `items` (a representative
+ * sample) with CUDA events, median of `reps` runs.  Installs the best tuning on the handle
+ * (read it with ops_handle_get_tuning), returns its thresholds in best[6] and the time in
+ * *best_ms.  Synchronizes.  No OpSparse counterpart: its tunables are compile-time
+ * constants (include/opsparse/utils/config.hpp:6-27). */
 int ops_autotune(ops_handle_t handle, int dtype, int32_t count, const ops_batch_item *items, int reps,
                  int32_t *best, float *best_ms, void *stream);
-/* Tuning records persisted as JSON {"<key>": [6 thresholds], ...}; key typically names the
- * GPU and the workload.  lookup returns OPS_NOT_SUPPORTED when the key is absent. */
+/* Tuning records persisted as JSON {"<key>": [values], ...}; key typically names the GPU and
+ * the workload.  ops_tuning_store / lookup keep the 6 thresholds; ops_tuning_store_record /
+ * lookup_record the whole ops_tuning (a thresholds-only record reads back with the other
+ * fields at their defaults).  The lookups return OPS_NOT_SUPPORTED when the key is absent. */
 int ops_tuning_store(const char *path, const char *key, const int32_t *thresholds);
 int ops_tuning_lookup(const char *path, const char *key, int32_t *thresholds);
+int ops_tuning_store_record(const char *path, const char *key, const ops_tuning *tuning);
+int ops_tuning_lookup_record(const char *path, const char *key, ops_tuning *tuning);
 
 /* Per-row intermediate-product counts (row_flop, rows_a int64, device; may be NULL) and
  * their sum (*total, host).  Synchronizes the stream. */

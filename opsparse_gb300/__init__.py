@@ -322,7 +322,8 @@ def batch_items(pairs):
 
 
 def autotune(handle: Handle, pairs, reps: int = 3, stream=None):
-    """Runs the library's autotuner on (a sample of) a workload; returns (thresholds, ms)."""
+    """Runs the library's autotuner on (a sample of) a workload and installs the best tuning
+    on the handle (handle.get_tuning() reads all of it); returns (thresholds, ms)."""
     torch = _torch()
     best = (C.c_int32 * 6)()
     ms = C.c_float(0)
@@ -341,3 +342,14 @@ def tuning_lookup(path: str, key: str):
     arr = (C.c_int32 * 6)()
     st = load().ops_tuning_lookup(str(path).encode(), key.encode(), arr)
     return list(arr) if st == capi.OPS_OK else None
+
+
+def tuning_store_record(path: str, key: str, tuning: dict) -> None:
+    """Stores a whole ops_tuning (as returned by Handle.get_tuning) under key."""
+    check(load().ops_tuning_store_record(str(path).encode(), key.encode(), C.byref(capi.Tuning.from_dict(tuning))))
+
+
+def tuning_lookup_record(path: str, key: str):
+    t = capi.Tuning()
+    st = load().ops_tuning_lookup_record(str(path).encode(), key.encode(), C.byref(t))
+    return t.as_dict() if st == capi.OPS_OK else None

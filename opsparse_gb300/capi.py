@@ -116,6 +116,8 @@ _SIGS = {
     "ops_autotune": (C.c_int, [P, C.c_int, I32, C.POINTER(BatchItem), C.c_int, C.POINTER(I32), C.POINTER(C.c_float), P]),
     "ops_tuning_store": (C.c_int, [C.c_char_p, C.c_char_p, C.POINTER(I32)]),
     "ops_tuning_lookup": (C.c_int, [C.c_char_p, C.c_char_p, C.POINTER(I32)]),
+    "ops_tuning_store_record": (C.c_int, [C.c_char_p, C.c_char_p, C.POINTER(Tuning)]),
+    "ops_tuning_lookup_record": (C.c_int, [C.c_char_p, C.c_char_p, C.POINTER(Tuning)]),
 }
 
 

@@ -879,12 +879,15 @@ extern "C" int ops_batch_destroy(ops_batch_t b)
 }
 
 // ---------------------------------------------------------------------- autotuner ----
-// Coordinate descent over the row-class thresholds {R8, R16, R32, W, E1, E2}: starting from
-// the handle's current values, each parameter in turn takes each of its candidate values
-// while the others stay fixed, and the fastest value is kept.  A candidate is timed with
-// CUDA events as the median of `reps` complete runs (plan + numeric) of the given batch;
-// pass a representative sample of the real workload.  The best thresholds are installed on
-// the handle and returned.
+// Coordinate descent over every field of ops_tuning: the row-class thresholds {R8, R16,
+// R32, W, E1, E2}, the warp-hash table's slots per output entry (hash-table size), the
+// batch plan (persistent kernels over row-size queues, or per segment) and the largest row
+// a warp takes in the persistent kernels (threads per row: a warp, or a 128- or 256-thread
+// CTA above it).  Starting from the handle's current tuning, each parameter in turn takes
+// each of its candidate values while the others stay fixed, and the fastest value is kept.
+// A candidate is timed with CUDA events as the median of `reps` complete runs (plan +
+// numeric) of the given batch; pass a representative sample of the real workload.  The
+// best tuning is installed on the handle; its thresholds are returned.
 namespace {
 
 float time_candidate(ops_handle_s *h, int dtype, int32_t count, const ops_batch_item *items, int reps,
@@ -914,6 +917,26 @@ float time_candidate(ops_handle_s *h, int dtype, int32_t count, const ops_batch_
     return ms[ms.size() / 2];
 }
 
+constexpr int kTuneParams = 9;  // 6 thresholds, hash_slots, batch_persistent, batch_warp_max
+
+void tuning_to_array(const ops_tuning &t, int *v)
+{
+    for (int i = 0; i < 6; ++i) v[i] = t.thresholds[i];
+    v[6] = t.hash_slots;
+    v[7] = t.batch_persistent;
+    v[8] = t.batch_warp_max;
+}
+
+ops_tuning tuning_from_array(const int *v)
+{
+    ops_tuning t{};
+    for (int i = 0; i < 6; ++i) t.thresholds[i] = v[i];
+    t.hash_slots = v[6];
+    t.batch_persistent = v[7];
+    t.batch_warp_max = v[8];
+    return t;
+}
+
 }  // namespace
 
 extern "C" int ops_autotune(ops_handle_t h, int dtype, int32_t count, const ops_batch_item *items, int reps,
@@ -921,38 +944,46 @@ extern "C" int ops_autotune(ops_handle_t h, int dtype, int32_t count, const ops_
 {
     if (!h || !items || count <= 0 || !best || reps < 1) return OPS_INVALID_ARGUMENT;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
-    const Thresholds saved = h->th;
-    int cur[6] = {h->th.r8, h->th.r16, h->th.r32, h->th.w, h->th.e1, h->th.e2};
-    const std::vector<std::vector<int>> cand = {
-        {8, 0}, {16, 0}, {32, 0}, {128, 64, 32, 0}, {1024, 512, 256, 0}, {13312, 4096}};
-    auto apply = [&](const int *v) { h->th = Thresholds{v[0], v[1], v[2], v[3], v[4], v[5]}; };
-    int status = OPS_OK;
-    apply(cur);
+    ops_tuning saved{};
+    OPS_CHECK(ops_handle_get_tuning(h, &saved));
+    int cur[kTuneParams];
+    tuning_to_array(saved, cur);
+    const std::vector<std::vector<int>> cand = {{8, 0},          {16, 0},       {32, 0}, {128, 64, 32, 0},
+                                                {1024, 512, 256, 0}, {13312, 4096}, {4, 2},  {1, 0},
+                                                {512, 256, 128}};
+    auto apply = [&](const int *v) {
+        const ops_tuning t = tuning_from_array(v);
+        return ops_handle_set_tuning(h, &t);
+    };
+    int status = apply(cur);
+    if (status != OPS_OK) return status;
     float best_t = time_candidate(h, dtype, count, items, reps, st, &status);
     if (status != OPS_OK) {
-        h->th = saved;
+        ops_handle_set_tuning(h, &saved);
         return status;
     }
-    for (int p = 0; p < 6; ++p) {
+    for (int p = 0; p < kTuneParams; ++p) {
         for (int v : cand[p]) {
             if (v == cur[p]) continue;
-            int trial[6];
+            int trial[kTuneParams];
             std::memcpy(trial, cur, sizeof(trial));
             trial[p] = v;
-            apply(trial);
+            status = apply(trial);
+            if (status != OPS_OK) break;
             const float t = time_candidate(h, dtype, count, items, reps, st, &status);
-            if (status != OPS_OK) {
-                h->th = saved;
-                return status;
-            }
+            if (status != OPS_OK) break;
             if (t < best_t) {
                 best_t = t;
                 std::memcpy(cur, trial, sizeof(cur));
             }
         }
+        if (status != OPS_OK) {
+            ops_handle_set_tuning(h, &saved);
+            return status;
+        }
     }
-    apply(cur);
-    std::memcpy(best, cur, sizeof(cur));
+    OPS_CHECK(apply(cur));
+    std::memcpy(best, cur, 6 * sizeof(int32_t));
     if (best_ms) *best_ms = best_t;
     return OPS_OK;
 }
@@ -1004,13 +1035,16 @@ std::vector<std::pair<std::string, std::vector<int>>> parse_records(const std::s
 
 }  // namespace
 
-extern "C" int ops_tuning_store(const char *path, const char *key, const int32_t *th)
+namespace {
+
+// Writes the record `key` = values[0..n) into the JSON file at path (other records kept).
+int store_values(const char *path, const char *key, const int *values, int n)
 {
-    if (!path || !key || !th) return OPS_INVALID_ARGUMENT;
+    if (!path || !key || !values) return OPS_INVALID_ARGUMENT;
     for (const char *c = key; *c; ++c)
         if (*c == '"' || *c == '\\') return OPS_INVALID_ARGUMENT;
     auto recs = parse_records(read_file(path));
-    std::vector<int> v(th, th + 6);
+    std::vector<int> v(values, values + n);
     bool found = false;
     for (auto &r : recs)
         if (r.first == key) {
@@ -1031,12 +1065,40 @@ extern "C" int ops_tuning_store(const char *path, const char *key, const int32_t
     return OPS_OK;
 }
 
+}  // namespace
+
+extern "C" int ops_tuning_store(const char *path, const char *key, const int32_t *th)
+{
+    return store_values(path, key, th, 6);
+}
+
 extern "C" int ops_tuning_lookup(const char *path, const char *key, int32_t *th)
 {
     if (!path || !key || !th) return OPS_INVALID_ARGUMENT;
     for (const auto &r : parse_records(read_file(path)))
-        if (r.first == key && r.second.size() == 6) {
+        if (r.first == key && r.second.size() >= 6) {
             std::memcpy(th, r.second.data(), 6 * sizeof(int32_t));
+            return OPS_OK;
+        }
+    return OPS_NOT_SUPPORTED;
+}
+
+extern "C" int ops_tuning_store_record(const char *path, const char *key, const ops_tuning *t)
+{
+    if (!t) return OPS_INVALID_ARGUMENT;
+    int v[kTuneParams];
+    tuning_to_array(*t, v);
+    return store_values(path, key, v, kTuneParams);
+}
+
+extern "C" int ops_tuning_lookup_record(const char *path, const char *key, ops_tuning *t)
+{
+    if (!path || !key || !t) return OPS_INVALID_ARGUMENT;
+    for (const auto &r : parse_records(read_file(path)))
+        if (r.first == key && (r.second.size() == 6 || r.second.size() == (size_t)kTuneParams)) {
+            int v[kTuneParams] = {0, 0, 0, 0, 0, 0, 4, 1, 512};  // fields a thresholds-only record lacks
+            std::memcpy(v, r.second.data(), r.second.size() * sizeof(int));
+            *t = tuning_from_array(v);
             return OPS_OK;
         }
     return OPS_NOT_SUPPORTED;

@@ -20,6 +20,22 @@ def test_tuning_store_roundtrip(tmp_path):
     assert json.loads(path.read_text())["gpu/y"][4] == 1024
 
 
+def test_tuning_record_store_roundtrip(tmp_path):
+    """Whole tuning records (thresholds, hash slots, batch plan, warp/CTA split) keep every
+    field; a thresholds-only record reads back with the other fields at their defaults, and
+    the thresholds of a whole record read back through the thresholds-only lookup."""
+    path = tmp_path / "tuning.json"
+    rec = {"thresholds": [8, 16, 32, 64, 512, 4096], "hash_slots": 2, "batch_persistent": 0, "batch_warp_max": 256}
+    ops.tuning_store_record(path, "gpu/batch", rec)
+    ops.tuning_store(path, "gpu/plain", [8, 16, 32, 128, 1024, 13312])
+    assert ops.tuning_lookup_record(path, "gpu/batch") == rec
+    assert ops.tuning_lookup(path, "gpu/batch") == rec["thresholds"]
+    assert ops.tuning_lookup_record(path, "gpu/plain") == {"thresholds": [8, 16, 32, 128, 1024, 13312],
+                                                           "hash_slots": 4, "batch_persistent": 1,
+                                                           "batch_warp_max": 512}
+    assert ops.tuning_lookup_record(path, "gpu/none") is None
+
+
 @pytest.mark.gpu
 def test_every_threshold_setting_gives_the_same_product(cuda):
     a = gen.web_powerlaw(40000, lmax=3000)
@@ -47,6 +63,8 @@ def test_autotune_installs_valid_thresholds(cuda):
     best, ms = ops.autotune(h, pairs, reps=1)
     assert len(best) == 6 and ms > 0
     assert h.get_thresholds() == best
+    t = h.get_tuning()  # every field the tuner searched holds one of its candidates
+    assert t["hash_slots"] in (2, 4) and t["batch_persistent"] in (0, 1) and t["batch_warp_max"] in (128, 256, 512)
     batch = ops.Batch(h, pairs)
     batch.execute(True)
     batch.check()
