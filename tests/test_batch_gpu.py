@@ -172,3 +172,45 @@ def test_hash_slots_give_the_same_product(cuda, slots):
     o = oracle.spgemm(*a, *b, ncols)
     assert np.array_equal(col, o[1]) and np.array_equal(val.view(np.uint64), o[2].view(np.uint64))
     h.close()
+
+
+def test_persistent_batch_wide_columns_and_empty_problems(cuda):
+    """The persistent path with 64-bit sort keys (a problem whose B has more than 2^20
+    columns) next to degenerate problems: a 0-row problem, a problem whose A has no
+    entries, and one whose B rows are all empty.  Every C_b equals its single call and the
+    oracle, bit for bit."""
+    import scipy.sparse as sp
+
+    rng = np.random.default_rng(31)
+
+    def csr(m):
+        m = sp.csr_matrix(m)
+        m.sort_indices()
+        return m.indptr.astype(np.int32), m.indices.astype(np.int32), m.data.astype(np.float64)
+
+    probs = []
+    # wide: 3,000 x 2,000 times 2,000 x 1,500,000 (about 40 products per row)
+    probs.append((csr(sp.random(3000, 2000, density=5 / 2000, random_state=rng)),
+                  csr(sp.random(2000, 1_500_000, density=8 / 1_500_000, random_state=rng)), 1_500_000))
+    probs.append((csr(sp.csr_matrix((0, 50))), csr(sp.random(50, 60, density=0.1, random_state=rng)), 60))
+    probs.append((csr(sp.csr_matrix((40, 30))), csr(sp.random(30, 70, density=0.2, random_state=rng)), 70))
+    probs.append((csr(sp.random(40, 30, density=0.2, random_state=rng)), csr(sp.csr_matrix((30, 70))), 70))
+    for n, a, b in make_batch(5, 17):
+        probs.append((a, b, n))
+    pairs = [(ops.csr_to_device(*a, len(a[0]) - 1, len(b[0]) - 1), ops.csr_to_device(*b, len(b[0]) - 1, nc))
+             for a, b, nc in probs]
+    h = ops.Handle()
+    batch = ops.Batch(h, pairs)
+    assert batch.queues()[0] is True
+    batch.execute(True)
+    batch.check()
+    single = ops.Handle()
+    for i, (a, b, nc) in enumerate(probs):
+        rpt, col, val = batch.result(i)
+        o = oracle.spgemm(*a, *b, nc)
+        assert np.array_equal(rpt.astype(np.int64), o[0]) and np.array_equal(col, o[1])
+        assert np.array_equal(val.view(np.uint64), o[2].view(np.uint64))
+        if len(a[0]) > 1:
+            s = single.spgemm(*pairs[i]).to_host()
+            assert np.array_equal(col, s[1]) and np.array_equal(val.view(np.uint64), s[2].view(np.uint64))
+    batch.close()
