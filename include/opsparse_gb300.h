@@ -132,8 +132,11 @@ const char *ops_handle_last_error(ops_handle_t handle);
 /* Rows handled by each sub-kernel in the last call (synchronises the handle's device
  * counters to the host): out[0..2] = E1 numeric rows by warp sort, warp hash and
  * expand/sort/compress; out[3..4] = E2 rows by the mid and the large expand/sort/compress
- * shape; out[5..6] = D rows by the whole-GPU sort and by the dense-row kernel.
- * Diagnostic; no OpSparse counterpart. */
+ * shape; out[5..6] = D rows by the whole-GPU sort and by the dense-row kernel;
+ * out[7..9] = expand rows of the numeric phase whose columns span fewer than 65,536
+ * columns, by path: column-window rank with no repeated column, rank with repeated
+ * columns re-folded, sort (more than 128 products in repeated columns).  Diagnostic; no
+ * OpSparse counterpart. */
 int ops_handle_subclass_rows(ops_handle_t handle, int32_t *out, int count);
 const char *ops_status_string(int status);
 

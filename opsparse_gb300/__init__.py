@@ -147,10 +147,12 @@ class Handle:
 
     def subclass_rows(self) -> dict:
         """Rows per sub-kernel of the last call: E1 numeric (warp sort, warp hash,
-        expand/sort/compress), E2 (mid, large shape) and D (whole-GPU sort, dense kernel)."""
-        arr = (C.c_int32 * 7)()
-        check(self.lib.ops_handle_subclass_rows(self.h, arr, 7), self.h)
-        return dict(zip(("e1_sort", "e1_hash", "e1_esc", "e2_mid", "e2_large", "d_sort", "d_dense"), list(arr)))
+        expand/sort/compress), E2 (mid, large shape), D (whole-GPU sort, dense kernel), and
+        the expand rows of narrow column span by path (rank, rank with re-fold, sorted)."""
+        arr = (C.c_int32 * 10)()
+        check(self.lib.ops_handle_subclass_rows(self.h, arr, 10), self.h)
+        return dict(zip(("e1_sort", "e1_hash", "e1_esc", "e2_mid", "e2_large", "d_sort", "d_dense", "rank",
+                         "rank_refold", "rank_sorted"), list(arr)))
 
     # -- two-phase ------------------------------------------------------------
     def symbolic(self, A: CsrMatrix, B: CsrMatrix, c_rpt=None, stream=None):

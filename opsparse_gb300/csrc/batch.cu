@@ -403,8 +403,8 @@ int launch_batch_symbolic(ops_batch_s *b, cudaStream_t st)
                 return launch_queue(b, 0, c, k_batch_count_rows<2 * kBatchWarpMax>, kBatchCountThreads,
                                     (size_t)W * 2 * kBatchWarpMax * sizeof(int), a, s);
             case kQE1:
-                return launch_queue(b, 0, c, k_batch_count_rows<2 * BescE1::kCap>, kBatchCountThreads,
-                                    (size_t)W * 2 * BescE1::kCap * sizeof(int), a, s);
+                return launch_queue(b, 0, c, k_batch_count_rows<2 * BescE1Batch::kCap>, kBatchCountThreads,
+                                    (size_t)W * 2 * BescE1Batch::kCap * sizeof(int), a, s);
             default:  // the table and the A-entry scan of EscMid's symbolic shape
                 return launch_queue(b, 0, c, k_batch_cta_count, EscMid::kThreads,
                                     (size_t)EscMid::kTable * 4 + (size_t)EscMid::kAEntries * 8, a, s);
@@ -426,11 +426,11 @@ int launch_batch_numeric(ops_batch_s *b, cudaStream_t st)
                 return launch_queue(b, 1, c, k_batch_warp_rows<16, T, KT>, WsortShape<16>::kThreads,
                                     WsortShape<16>::smem<true, T, KT>(), a, s);
             case kQE1:
-                return launch_queue(b, 1, c, k_batch_cta_rows<BescE1, true, T, KT>, BescE1::kThreads,
-                                    BescE1::smem<true, KT>(), a, s);
+                return launch_queue(b, 1, c, k_batch_cta_rows<BescE1Batch, true, T, KT>, BescE1Batch::kThreads,
+                                    BescE1Batch::smem<true, KT, T>(), a, s);
             default:
-                return launch_queue(b, 1, c, k_batch_cta_rows<BescMid, true, T, KT>, BescMid::kThreads,
-                                    BescMid::smem<true, KT>(), a, s);
+                return launch_queue(b, 1, c, k_batch_cta_rows<BescMidRank, true, T, KT>, BescMidRank::kThreads,
+                                    BescMidRank::smem<true, KT, T>(), a, s);
         }
     });
 }
@@ -540,7 +540,7 @@ int plan_persistent(ops_batch_s *b, ops_handle_s *h, size_t vs, cudaStream_t st,
         num[i] = seg_args<double>(s);  // the value pointers are reinterpreted by the value type
     }
     OPS_CUDA(h, cudaMemcpyAsync(b->d_num, num.data(), sizeof(SpgemmArgs<double>) * nseg, cudaMemcpyHostToDevice, st));
-    b->key64 = max_n > (1 << (32 - BescMid::kIdBits));  // the widest product index of the numeric keys
+    b->key64 = max_n > (1 << (32 - BescMidRank::kIdBits));  // the widest product index of the numeric keys
     b->persistent = true;
     used = true;
     return OPS_OK;

@@ -39,7 +39,7 @@ constexpr int kBatchChunk = 8;        // warp-queue rows a warp takes per cursor
 constexpr int kBatchMaxSegs = 16;     // segments one persistent launch covers (their arguments sit in shared memory)
 constexpr int kBatchCountThreads = 256;
 static_assert(WsortShape<4>::kMax == kBatchQ128 && WsortShape<16>::kMax == kBatchWarpMax, "warp-queue capacities");
-static_assert(EscMid::kProducts >= BescMid::kCap && EscMid::kAEntries >= BescMid::kAEntries, "kQMid rows fit both shapes");
+static_assert(EscMid::kProducts >= BescMidRank::kCap && EscMid::kAEntries >= BescMidRank::kAEntries, "kQMid rows fit both shapes");
 
 enum BatchQueue : int { kQ128 = 0, kQWarp = 1, kQE1 = 2, kQMid = 3, kQBeyond = 4, kNumBatchQueues = 4 };
 
@@ -99,8 +99,8 @@ static __global__ void __launch_bounds__(256) k_batch_setup(const SpgemmArgs<dou
             if (flop == 0) g.c_rpt[r] = 0;
             else if (flop <= kBatchQ128) cls = kQ128;
             else if (flop <= warp_max) cls = kQWarp;
-            else if (flop <= BescE1::kCap && lenA <= BescE1::kAEntries) cls = kQE1;
-            else if (flop <= BescMid::kCap && lenA <= BescMid::kAEntries) cls = kQMid;
+            else if (flop <= BescE1Batch::kCap && lenA <= BescE1Batch::kAEntries) cls = kQE1;
+            else if (flop <= BescMidRank::kCap && lenA <= BescMidRank::kAEntries) cls = kQMid;
             else cls = kQBeyond;
         }
 #pragma unroll
@@ -281,10 +281,11 @@ __global__ void __launch_bounds__(Shape::kThreads, Shape::kMinBlocks)
     __shared__ int s_warp_sums[32];
     __shared__ KT s_last[32];
     __shared__ int s_unit;
-    __shared__ unsigned s_bad;
-    if (threadIdx.x == 0) s_bad = 0u;
+    __shared__ BescScratch s_sc;
+    if (threadIdx.x == 0) s_sc.reset();
     batch_load_segs<T>(segs, seg_row_base, nseg, s_segs, s_base);
-    const BescSmem<Shape, kNum, KT> sm(smem_raw);
+    const BescSmem<Shape, kNum, KT, T> sm(smem_raw);
+    sm.init();
     const int n = *count;
     unsigned long long nnz_unused = 0;
     for (;;) {
@@ -295,7 +296,7 @@ __global__ void __launch_bounds__(Shape::kThreads, Shape::kMinBlocks)
         if (u >= n) break;
         const int gr = __ldg(queue + u);
         const int s = batch_segment(s_base, nseg, gr);
-        besc_row<Shape, kNum, T, KT>(s_segs[s], gr - s_base[s], sm, s_warp_sums, s_last, &s_bad, nnz_unused);
+        besc_row<Shape, kNum, T, KT>(s_segs[s], gr - s_base[s], sm, s_warp_sums, s_last, &s_sc, nnz_unused);
     }
 }
 

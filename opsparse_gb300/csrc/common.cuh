@@ -97,6 +97,8 @@ struct DevInfo {
     unsigned long long d_len_a;   // A entries of the D rows
     unsigned long long d_flop;    // products of the D rows
     int d_cursor;                 // long runs listed by the D-row short-run fold
+    int rank_rows[3];             // CTA expand rows by the column-window rank path: [no late
+                                  // products, late products re-folded, too many late: sorted]
 };
 
 // Arguments shared by every SpGEMM kernel.

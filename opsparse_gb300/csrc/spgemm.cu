@@ -46,11 +46,11 @@ template <typename Shape, typename T>
 void set_besc_attrs()
 {
     cudaFuncSetAttribute(k_besc_rows<Shape, true, T, unsigned>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)Shape::template smem<true, unsigned>());
+                         (int)Shape::template smem<true, unsigned, T>());
     cudaFuncSetAttribute(k_besc_rows<Shape, true, T, unsigned long long>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)Shape::template smem<true, unsigned long long>());
+                         (int)Shape::template smem<true, unsigned long long, T>());
     cudaFuncSetAttribute(k_besc_rows<Shape, false, T, unsigned>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)Shape::template smem<false, unsigned>());
+                         (int)Shape::template smem<false, unsigned, T>());
 }
 
 // Launch the CTA-per-row bitonic kernel of `Shape` on `s`: numeric keys pack the product
@@ -61,13 +61,13 @@ void launch_besc(const SpgemmArgs<T> &g, const int *list, const int *count_ptr, 
 {
     if (!kNum) {
         k_besc_rows<Shape, false, T, unsigned>
-            <<<grid, Shape::kThreads, Shape::template smem<false, unsigned>(), s>>>(g, list, count_ptr, cursor);
+            <<<grid, Shape::kThreads, Shape::template smem<false, unsigned, T>(), s>>>(g, list, count_ptr, cursor);
     } else if (ceil_log2(std::max(g.N, 2)) + Shape::kIdBits <= 32) {
         k_besc_rows<Shape, true, T, unsigned>
-            <<<grid, Shape::kThreads, Shape::template smem<true, unsigned>(), s>>>(g, list, count_ptr, cursor);
+            <<<grid, Shape::kThreads, Shape::template smem<true, unsigned, T>(), s>>>(g, list, count_ptr, cursor);
     } else {
         k_besc_rows<Shape, true, T, unsigned long long>
-            <<<grid, Shape::kThreads, Shape::template smem<true, unsigned long long>(), s>>>(g, list, count_ptr,
+            <<<grid, Shape::kThreads, Shape::template smem<true, unsigned long long, T>(), s>>>(g, list, count_ptr,
                                                                                              cursor);
     }
 }
@@ -978,7 +978,7 @@ const char *ops_handle_last_error(ops_handle_t h) { return h ? h->last_error.c_s
 int ops_handle_subclass_rows(ops_handle_t h, int32_t *out, int n)
 {
     if (!h || !out || n < 0) return OPS_INVALID_ARGUMENT;
-    int v[7] = {};
+    int v[10] = {};
     v[5] = h->d_rows_path[0];
     v[6] = h->d_rows_path[1];
     if (h->info) {
@@ -990,8 +990,9 @@ int ops_handle_subclass_rows(ops_handle_t h, int32_t *out, int n)
         v[2] = d.split[2] + d.split1[2];
         v[3] = d.split2[0];
         v[4] = d.split2[1];
+        for (int i = 0; i < 3; ++i) v[7 + i] = d.rank_rows[i];
     }
-    for (int i = 0; i < n && i < 7; ++i) out[i] = v[i];
+    for (int i = 0; i < n && i < 10; ++i) out[i] = v[i];
     return OPS_OK;
 }
 
