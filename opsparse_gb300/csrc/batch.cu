@@ -399,9 +399,9 @@ int launch_batch_symbolic(ops_batch_s *b, cudaStream_t st)
             case kQ128:
                 return launch_queue(b, 0, c, k_batch_count_rows<2 * kBatchQ128>, kBatchCountThreads,
                                     (size_t)W * 2 * kBatchQ128 * sizeof(int), a, s);
-            case kQWarp:
-                return launch_queue(b, 0, c, k_batch_count_rows<2 * kBatchWarpMax>, kBatchCountThreads,
-                                    (size_t)W * 2 * kBatchWarpMax * sizeof(int), a, s);
+            case kQWarp:  // twice the table a row needs: room for the wide column window
+                return launch_queue(b, 0, c, k_batch_count_rows<4 * kBatchWarpMax>, kBatchCountThreads,
+                                    (size_t)W * 4 * kBatchWarpMax * sizeof(int), a, s);
             case kQE1:
                 return launch_queue(b, 0, c, k_batch_count_rows<2 * BescE1Batch::kCap>, kBatchCountThreads,
                                     (size_t)W * 2 * BescE1Batch::kCap * sizeof(int), a, s);

@@ -189,8 +189,10 @@ __device__ __forceinline__ int warp_hash_count(const SpgemmArgs<double> &g, int 
 // Symbolic persistent kernel of a warp queue (rows of at most TMAX/2 products): every warp
 // counts kBatchChunk rows per cursor step in its own table of at most TMAX slots.  Rows of
 // at most 32 A entries whose B rows are long (16 or more products per A entry) and whose
-// products fall within kWinBits consecutive columns are counted over a window bitmap in
-// the same space instead (window_row_short, kernels.cuh), when it is large enough.
+// products fall within one window of consecutive columns are counted over a window bitmap
+// in the same space instead (window_row_short, kernels.cuh), when it is large enough: a
+// window of kWinBits columns, or twice that where the table space is 2 * kWinWords words
+// (one marking OR per product and a sweep of the window's words, no hash probes).
 template <int TMAX>
 __global__ void __launch_bounds__(kBatchCountThreads) k_batch_count_rows(const SpgemmArgs<double> *__restrict__ segs,
                                                                          const int *__restrict__ seg_row_base,
@@ -198,6 +200,7 @@ __global__ void __launch_bounds__(kBatchCountThreads) k_batch_count_rows(const S
                                                                          const int *count, int *cursor)
 {
     constexpr bool kWindow = TMAX >= kWinWords;  // the table's space holds the window bitmap
+    constexpr int kWB = TMAX >= 2 * kWinWords ? 2 * kWinBits : kWinBits;  // window columns
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ SpgemmArgs<double> s_segs[kBatchMaxSegs];
     __shared__ int s_base[kBatchMaxSegs + 1];
@@ -223,8 +226,8 @@ __global__ void __launch_bounds__(kBatchCountThreads) k_batch_count_rows(const S
             if (kWindow && flop >= 16 * (a1 - a0) && a1 - a0 <= 32) {
                 const int nnz_b = __ldg(g.brpt + g.K);
                 const bool bcol16 = ((size_t)g.bcol & 15) == 0;
-                if (window_row_short<double>(g, r, a0, a1, nnz_b, bcol16, reinterpret_cast<unsigned *>(keys),
-                                             win_clean, nnz_unused))
+                if (window_row_short<double, kWB>(g, r, a0, a1, nnz_b, bcol16, reinterpret_cast<unsigned *>(keys),
+                                                  win_clean, nnz_unused))
                     continue;
             }
             win_clean = false;  // the hash table reuses the space
@@ -280,23 +283,28 @@ __global__ void __launch_bounds__(Shape::kThreads, Shape::kMinBlocks)
     __shared__ int s_base[kBatchMaxSegs + 1];
     __shared__ int s_warp_sums[32];
     __shared__ KT s_last[32];
-    __shared__ int s_unit;
+    __shared__ int s_draw[2];
     __shared__ BescScratch s_sc;
-    if (threadIdx.x == 0) s_sc.reset();
+    if (threadIdx.x == 0) {
+        s_sc.reset();
+        s_draw[0] = atomicAdd(cursor, 1);
+    }
     batch_load_segs<T>(segs, seg_row_base, nseg, s_segs, s_base);
     const BescSmem<Shape, kNum, KT, T> sm(smem_raw);
     sm.init();
+    __syncthreads();
     const int n = *count;
     unsigned long long nnz_unused = 0;
-    for (;;) {
-        if (threadIdx.x == 0) s_unit = atomicAdd(cursor, 1);
-        __syncthreads();
-        const int u = s_unit;
-        __syncthreads();
+    // thread 0 draws the next queue entry while the CTA works on the current one (two
+    // slots, published by the row's closing barrier)
+    for (int it = 0;; ++it) {
+        const int u = s_draw[it & 1];
         if (u >= n) break;
+        const int next = threadIdx.x == 0 ? atomicAdd(cursor, 1) : 0;
         const int gr = __ldg(queue + u);
         const int s = batch_segment(s_base, nseg, gr);
-        besc_row<Shape, kNum, T, KT>(s_segs[s], gr - s_base[s], sm, s_warp_sums, s_last, &s_sc, nnz_unused);
+        besc_row<Shape, kNum, T, KT>(s_segs[s], gr - s_base[s], sm, s_warp_sums, s_last, &s_sc, nnz_unused,
+                                     &s_draw[(it + 1) & 1], next);
     }
 }
 

@@ -90,10 +90,12 @@ using BescMidRank = BescShape<256, 16, 1280, 3, true>;  // the batch's rows of 1
 // besc_row leaves it reset on return.
 struct BescScratch {
     unsigned bad;   // a B column outside [0, N) was seen
-    unsigned cmin;  // the row's smallest and largest column (rank path)
-    unsigned cmax;
+    unsigned cmin;  // the row's column window (rank path): the smallest first column and the
+    unsigned cmax;  // largest last column of its B rows
     int late;       // late products of the row
     int listed;     // late products listed so far (rank path)
+    int n;          // the row's products (rank path's scan)
+    unsigned wbad;  // a product outside the window (unsorted B row): the row takes the sort
     __device__ __forceinline__ void reset()
     {
         bad = 0u;
@@ -101,6 +103,8 @@ struct BescScratch {
         cmax = 0u;
         late = 0;
         listed = 0;
+        n = 0;
+        wbad = 0u;
     }
 };
 
@@ -388,15 +392,28 @@ __device__ __forceinline__ void besc_rank_refold(const SpgemmArgs<T> &g, int a0,
     __syncthreads();
 }
 
-// Rank path of one numeric row (n products, keys in skeys; sc->cmin/cmax the row's column
-// range, spanning fewer than kRankWinBits columns; the window bitmap all zero).  Returns
-// the row's entry count, or -1 when the row has more late products than kRankLateMax (the
-// keys are then untouched and the caller sorts).  Leaves the bitmap all zero.
-// Block-uniform; every thread calls it.
+// 128-word chunks of the window bitmap a rank-path row uses.
+__device__ __forceinline__ int besc_rank_chunks(const BescScratch *sc)
+{
+    return (int)(((sc->cmax - sc->cmin) >> 5) / kRankChunk) + 1;
+}
+
+// Clears the first nchunks chunks of the window bitmap (all threads of the CTA).
+__device__ __forceinline__ void besc_rank_clear(unsigned *bm, int nchunks)
+{
+    uint4 *bm4 = reinterpret_cast<uint4 *>(bm);
+    for (int i = threadIdx.x; i < nchunks * (kRankChunk / 4); i += blockDim.x) bm4[i] = make_uint4(0u, 0u, 0u, 0u);
+}
+
+// Rank path of one numeric row, after the expansion marked the window bitmap (n products,
+// keys in skeys; sc->cmin/cmax the row's column window, spanning fewer than kRankWinBits
+// columns; `late` = this thread's late products, bit k for product tid + k * NT; n_late
+// the row's count, at most kRankLateMax).  Returns the row's entry count and leaves the
+// bitmap all zero.  Block-uniform; every thread calls it.
 template <typename Shape, int kIdBits, typename T, typename KT>
 __device__ __forceinline__ int besc_rank_fold(const SpgemmArgs<T> &g, int n, int a0,
                                               const BescSmem<Shape, true, KT, T> &sm, BescScratch *sc,
-                                              int *s_warp_sums, int off, int n_expect)
+                                              int *s_warp_sums, int off, int n_expect, unsigned late, int n_late)
 {
     using AccT = Acc<T>;
     constexpr int NT = Shape::kThreads;
@@ -407,37 +424,13 @@ __device__ __forceinline__ int besc_rank_fold(const SpgemmArgs<T> &g, int n, int
     const int lane = lane_id();
     const int warp = tid >> 5;
     const unsigned cmin = sc->cmin;
-    const int nw = (int)((sc->cmax - cmin) >> 5) + 1;
-    const int nchunks = (nw + kRankChunk - 1) / kRankChunk;
+    const int nchunks = besc_rank_chunks(sc);
     uint4 *bm4 = reinterpret_cast<uint4 *>(sm.bm);
-    auto clear_bitmap = [&] {
-        for (int i = tid; i < nchunks * (kRankChunk / 4); i += NT) bm4[i] = make_uint4(0u, 0u, 0u, 0u);
-    };
     unsigned col[PER];
 #pragma unroll
     for (int k = 0; k < PER; ++k) {
         const int q = tid + k * NT;
         col[k] = q < n ? (unsigned)(sm.skeys[bpad(q)] >> kIdBits) : 0u;
-    }
-    // 1. window bitmap; a set bit seen by the OR marks the product late
-    unsigned late = 0u;
-#pragma unroll
-    for (int k = 0; k < PER; ++k) {
-        const int q = tid + k * NT;
-        if (q < n) {
-            const unsigned d = col[k] - cmin;
-            const unsigned bit = 1u << (d & 31u);
-            const unsigned old = atomicOr(&sm.bm[d >> 5], bit);
-            late |= (old & bit) ? (1u << k) : 0u;
-        }
-    }
-    const int nl = (int)__reduce_add_sync(kFull, (unsigned)__popc(late));
-    if (lane == 0 && nl) atomicAdd(&sc->late, nl);
-    __syncthreads();
-    const int n_late = sc->late;
-    if (n_late > kRankLateMax) {
-        clear_bitmap();  // before the row's closing barrier
-        return -1;
     }
     // 2. prefix popcounts: each warp sweeps a contiguous run of 128-word chunks, a lane
     //    four words at a time (counts, barrier, then prefixes)
@@ -531,20 +524,103 @@ __device__ __forceinline__ int besc_rank_fold(const SpgemmArgs<T> &g, int n, int
             g.c_val[off + i] = sm.rval[i];
         }
     }
-    clear_bitmap();
+    besc_rank_clear(sm.bm, nchunks);
     return total;
+}
+
+// Scan of A's row for the rank shapes: the B-row lengths into s_incl / s_b0 (as
+// esc_scan_row) and the row's column window from the B rows' first and last columns
+// (B rows are sorted) into sc->cmin / cmax.  Rows of at most 128 A entries are scanned by
+// warp 0 alone, four entries a lane with their loads in flight together; longer rows by
+// the CTA.  Returns the product count on every thread; ends with a barrier.
+template <int NT, typename T>
+__device__ __forceinline__ int besc_rank_scan_row(const SpgemmArgs<T> &g, int a0, int lenA, int *s_incl,
+                                                  int *s_b0, int *s_warp_sums, BescScratch *sc)
+{
+    const int tid = threadIdx.x;
+    const int lane = lane_id();
+    if (lenA > 128) {
+        unsigned lo = 0xffffffffu, hi = 0u;
+        for (int q = tid; q < lenA; q += NT) {
+            const int j = __ldg(g.acol + a0 + q);
+            const int b0 = __ldg(g.brpt + j), b1 = __ldg(g.brpt + j + 1);
+            if (b1 > b0) {
+                lo = min(lo, (unsigned)__ldg(g.bcol + b0));
+                hi = max(hi, (unsigned)__ldg(g.bcol + b1 - 1));
+            }
+        }
+        lo = __reduce_min_sync(kFull, lo);
+        hi = __reduce_max_sync(kFull, hi);
+        if (lane == 0 && lo <= hi) {
+            atomicMin(&sc->cmin, lo);
+            atomicMax(&sc->cmax, hi);
+        }
+        return esc_scan_row<NT, T>(g, a0, lenA, s_incl, s_b0, s_warp_sums);  // ends with a barrier
+    }
+    if (tid < 32) {
+        int b0[4], b1[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const int q = u * 32 + lane;
+            b0[u] = q < lenA ? __ldg(g.acol + a0 + q) : -1;  // A's column, then B's row start
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const int j = b0[u];
+            b0[u] = j >= 0 ? __ldg(g.brpt + j) : 0;
+            b1[u] = j >= 0 ? __ldg(g.brpt + j + 1) : 0;
+        }
+        unsigned lo = 0xffffffffu, hi = 0u;
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            if (b1[u] > b0[u]) {
+                lo = min(lo, (unsigned)__ldg(g.bcol + b0[u]));
+                hi = max(hi, (unsigned)__ldg(g.bcol + b1[u] - 1));
+            }
+        }
+        int running = 0;
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const int q = u * 32 + lane;
+            int incl = b1[u] - b0[u];
+#pragma unroll
+            for (int d = 1; d < 32; d <<= 1) {
+                const int t = __shfl_up_sync(kFull, incl, d);
+                if (lane >= d) incl += t;
+            }
+            if (q < lenA) {
+                s_incl[q] = running + incl;
+                s_b0[q] = b0[u];
+            }
+            running += __shfl_sync(kFull, incl, 31);
+        }
+        lo = __reduce_min_sync(kFull, lo);
+        hi = __reduce_max_sync(kFull, hi);
+        if (lane == 0) {
+            sc->n = running;
+            if (lo <= hi) {
+                sc->cmin = lo;
+                sc->cmax = hi;
+            }
+        }
+    }
+    __syncthreads();
+    return sc->n;
 }
 
 // One row r (at most Shape::kCap products, Shape::kAEntries A entries) by the whole CTA:
 // expand, sort (or rank), then count (symbolic) or fold and write (numeric).  Symbolic and
 // one-pass calls write the row's count to c_rpt[r]; the count is also added to nnz_acc
 // (thread 0).  s_warp_sums (32 ints), s_last (32 keys) and sc are block-shared scratch;
-// sc must be reset on entry and is reset again on return.  Every thread of the CTA calls
-// it; it ends with a barrier.
+// sc must be reset on entry and is reset again on return.  Thread 0 stores publish_val to
+// *publish before the closing barrier (the caller's draw of its next row).  Every thread
+// of the CTA calls it; it ends with a barrier.  Rank shapes: when the row's column window (known from the
+// scan) spans fewer than kRankWinBits columns, the expansion also marks each product's
+// column in the window bitmap, so the rank path starts at its prefix sweep.
 template <typename Shape, bool kNum, typename T, typename KT>
 __device__ __forceinline__ void besc_row(const SpgemmArgs<T> &g, int r, const BescSmem<Shape, kNum, KT, T> &sm,
                                          int *s_warp_sums, KT *s_last, BescScratch *sc,
-                                         unsigned long long &nnz_acc)
+                                         unsigned long long &nnz_acc, int *publish, int publish_val)
 {
     constexpr int NT = Shape::kThreads;
     constexpr int kIdBits = kNum ? Shape::kIdBits : 0;
@@ -554,7 +630,17 @@ __device__ __forceinline__ void besc_row(const SpgemmArgs<T> &g, int r, const Be
     const int warp = tid >> 5;
     const int a0 = __ldg(g.arpt + r);
     const int lenA = __ldg(g.arpt + r + 1) - a0;
-    const int n = esc_scan_row<NT, T>(g, a0, lenA, sm.s_incl, sm.s_b0, s_warp_sums);
+    int n;
+    bool rank_ok = false;
+    unsigned cmin = 0u, span = 0u;
+    if constexpr (kRank) {
+        n = besc_rank_scan_row<NT, T>(g, a0, lenA, sm.s_incl, sm.s_b0, s_warp_sums, sc);
+        cmin = sc->cmin;
+        span = sc->cmax - cmin;
+        rank_ok = n > 0 && n <= Shape::kCap && sc->cmin <= sc->cmax && span < (unsigned)kRankWinBits;
+    } else {
+        n = esc_scan_row<NT, T>(g, a0, lenA, sm.s_incl, sm.s_b0, s_warp_sums);
+    }
     int off = 0, n_expect = 0;
     if constexpr (kNum) {
         if (g.soff) {  // one-pass: the row's staging slot, count unknown
@@ -565,10 +651,11 @@ __device__ __forceinline__ void besc_row(const SpgemmArgs<T> &g, int r, const Be
             n_expect = __ldg(g.c_rpt + r + 1) - off;
         }
     }
-    // expansion: kUnroll chunks of 32 products per warp, loads in flight together
-    bool bad = false;
-    unsigned lo = 0xffffffffu, hi = 0u;
-    for (int c0 = warp * 32; c0 < n; c0 += kUnroll * NT) {
+    // expansion: kUnroll chunks of 32 products per warp, loads in flight together; product
+    // q = tid + k * NT is this thread's k-th (k = step * kUnroll + u)
+    bool bad = false, wbad = false;
+    unsigned late = 0u;
+    for (int c0 = warp * 32, kb = 0; c0 < n; c0 += kUnroll * NT, kb += kUnroll) {
         int oo[kUnroll], kk[kUnroll];
         bool v[kUnroll];
 #pragma unroll
@@ -589,17 +676,23 @@ __device__ __forceinline__ void besc_row(const SpgemmArgs<T> &g, int r, const Be
             sm.skeys[bpad(q)] = ((KT)(unsigned)col[u] << kIdBits) | (KT)(kNum ? q : 0);
             if constexpr (kNum) sm.own[q] = (unsigned short)oo[u];
             if constexpr (kRank) {
-                lo = min(lo, (unsigned)col[u]);
-                hi = max(hi, (unsigned)col[u]);
+                if (rank_ok) {
+                    const unsigned d = (unsigned)col[u] - cmin;
+                    if (d <= span) {
+                        const unsigned bit = 1u << (d & 31u);
+                        if (atomicOr(&sm.bm[d >> 5], bit) & bit) late |= 1u << (kb + u);
+                    } else {
+                        wbad = true;
+                    }
+                }
             }
         }
     }
     if constexpr (kRank) {
-        lo = __reduce_min_sync(kFull, lo);
-        hi = __reduce_max_sync(kFull, hi);
-        if (lane == 0 && lo <= hi) {
-            atomicMin(&sc->cmin, lo);
-            atomicMax(&sc->cmax, hi);
+        if (rank_ok) {
+            const int nl = (int)__reduce_add_sync(kFull, (unsigned)__popc(late));
+            if (lane == 0 && nl) atomicAdd(&sc->late, nl);
+            if (wbad) sc->wbad = 1u;
         }
     }
     if (bad) sc->bad = 1u;
@@ -609,9 +702,15 @@ __device__ __forceinline__ void besc_row(const SpgemmArgs<T> &g, int r, const Be
     constexpr int P = Shape::kPMax;
     int total = -1;
     if constexpr (kRank) {
-        if (n > 0 && n <= Shape::kCap && sc->cmin <= sc->cmax && sc->cmax - sc->cmin < (unsigned)kRankWinBits) {
-            total = besc_rank_fold<Shape, kIdBits, T, KT>(g, n, a0, sm, sc, s_warp_sums, off, n_expect);
-            if (tid == 0) atomicAdd(&g.info->rank_rows[total < 0 ? 2 : (sc->late ? 1 : 0)], 1);
+        if (rank_ok) {
+            const int n_late = sc->late;
+            if (n_late > kRankLateMax || sc->wbad) {
+                besc_rank_clear(sm.bm, besc_rank_chunks(sc));  // the sort takes the row
+            } else {
+                total = besc_rank_fold<Shape, kIdBits, T, KT>(g, n, a0, sm, sc, s_warp_sums, off, n_expect, late,
+                                                              n_late);
+            }
+            if (tid == 0) atomicAdd(&g.info->rank_rows[total < 0 ? 2 : (n_late ? 1 : 0)], 1);
         }
     }
     if (total >= 0) {
@@ -634,6 +733,7 @@ __device__ __forceinline__ void besc_row(const SpgemmArgs<T> &g, int r, const Be
             nnz_acc += (unsigned long long)total;
         }
     }
+    if (tid == 0) *publish = publish_val;
     __syncthreads();
     if (tid == 0) sc->reset();  // read by every thread before the barrier above
 }
@@ -646,21 +746,26 @@ __global__ void __launch_bounds__(Shape::kThreads, Shape::kMinBlocks) k_besc_row
     const int tid = threadIdx.x;
     __shared__ int s_warp_sums[32];
     __shared__ KT s_last[32];
-    __shared__ int s_row;
+    __shared__ int s_draw[2];
     __shared__ BescScratch s_sc;
     const BescSmem<Shape, kNum, KT, T> sm(smem_raw);
 
     const int count = *count_ptr;
     unsigned long long nnz_acc = 0;
-    if (tid == 0) s_sc.reset();
+    if (tid == 0) {
+        s_sc.reset();
+        s_draw[0] = atomicAdd(cursor, 1);
+    }
     sm.init();
-    for (;;) {
-        if (tid == 0) s_row = atomicAdd(cursor, 1);
-        __syncthreads();
-        const int it = s_row;
-        __syncthreads();
-        if (it >= count) break;
-        besc_row<Shape, kNum, T, KT>(g, __ldg(list + it), sm, s_warp_sums, s_last, &s_sc, nnz_acc);
+    __syncthreads();
+    // thread 0 draws the next row while the CTA works on the current one; two slots, so
+    // the draw is published by the row's closing barrier
+    for (int it = 0;; ++it) {
+        const int u = s_draw[it & 1];
+        if (u >= count) break;
+        const int next = tid == 0 ? atomicAdd(cursor, 1) : 0;
+        besc_row<Shape, kNum, T, KT>(g, __ldg(list + u), sm, s_warp_sums, s_last, &s_sc, nnz_acc,
+                                     &s_draw[(it + 1) & 1], next);
     }
     if (tid == 0 && nnz_acc) atomicAdd(&g.info->total_nnz, nnz_acc);
 }

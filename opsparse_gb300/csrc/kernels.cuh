@@ -856,13 +856,14 @@ __device__ __forceinline__ void window_load_quads(const int *__restrict__ bcol, 
 // loads of its first and last column that give the window: a stencil row (B rows of 27
 // columns) takes three dependent round trips to L2 (A's column, B's row extent, B's
 // columns), where finding the window before reading the B rows takes at least four.
-// Returns false, having marked nothing, when the products do not fit a window of kWinBits
-// columns.
-template <typename T>
+// Returns false, having marked nothing, when the products do not fit a window of WBITS
+// columns (bits holds WBITS / 32 words).
+template <typename T, int WBITS = kWinBits>
 __device__ __forceinline__ bool window_row_short(const SpgemmArgs<T> &g, int r, int a0, int a1, int nnz_b,
                                                  bool bcol16, unsigned *bits, bool &clean,
                                                  unsigned long long &nnz_acc)
 {
+    static_assert(WBITS % 128 == 0, "whole 16-byte sweep steps");
     const int lane = lane_id();
     int b0 = 0, b1 = 0;
     if (a0 + lane < a1) {
@@ -876,9 +877,9 @@ __device__ __forceinline__ bool window_row_short(const SpgemmArgs<T> &g, int r, 
     window_load_quads(g.bcol, q0, b0, b1, vec, v);
     const int cmin = __reduce_min_sync(kFull, b1 > b0 ? __ldg(g.bcol + b0) : INT_MAX);
     const int cmax = __reduce_max_sync(kFull, b1 > b0 ? __ldg(g.bcol + b1 - 1) : -1);
-    if (!(cmax >= cmin && cmax - cmin < kWinBits)) return false;
+    if (!(cmax >= cmin && cmax - cmin < WBITS)) return false;
     if (!clean) {
-        for (int i = lane; i < kWinWords; i += 32) bits[i] = 0u;
+        for (int i = lane; i < WBITS / 32; i += 32) bits[i] = 0u;
         __syncwarp();
         clean = true;
     }
