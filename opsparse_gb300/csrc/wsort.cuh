@@ -31,8 +31,10 @@ struct WsortShape {
     static constexpr int kWarps = PMAX <= 4 ? 8 : 4;           // warps per CTA
     static constexpr int kThreads = 32 * kWarps;
     // CTAs per SM the registers must allow: 4 for both the 128-key variant (8 warps per
-    // CTA, 64 registers) and the 32-key symbolic variant (128 registers)
-    static constexpr int kMinBlocks = PMAX >= 32 ? 4 : (PMAX <= 4 ? 4 : 1);
+    // CTA, 64 registers) and the 32-key symbolic variant (128 registers); 5 for the
+    // 512-key variant (at most 102 registers; with no bound it took 103-127, which left 4
+    // CTAs, and measured slower on both the web graph and the batch)
+    static constexpr int kMinBlocks = PMAX >= 32 ? 4 : (PMAX <= 4 ? 4 : 5);
     static constexpr int kIdBits = PMAX <= 4 ? 7 : (PMAX <= 8 ? 8 : (PMAX <= 16 ? 9 : 10));
     static constexpr int kKeySlots = kMax + kMax / 32;         // padded key array
     static constexpr int kHeadSlots = kMax + 32;               // run heads + end marker
