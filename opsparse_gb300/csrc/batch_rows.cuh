@@ -283,28 +283,23 @@ __global__ void __launch_bounds__(Shape::kThreads, Shape::kMinBlocks)
     __shared__ int s_base[kBatchMaxSegs + 1];
     __shared__ int s_warp_sums[32];
     __shared__ KT s_last[32];
-    __shared__ int s_draw[2];
+    __shared__ int s_unit;
     __shared__ BescScratch s_sc;
-    if (threadIdx.x == 0) {
-        s_sc.reset();
-        s_draw[0] = atomicAdd(cursor, 1);
-    }
+    if (threadIdx.x == 0) s_sc.reset();
     batch_load_segs<T>(segs, seg_row_base, nseg, s_segs, s_base);
     const BescSmem<Shape, kNum, KT, T> sm(smem_raw);
     sm.init();
-    __syncthreads();
     const int n = *count;
     unsigned long long nnz_unused = 0;
-    // thread 0 draws the next queue entry while the CTA works on the current one (two
-    // slots, published by the row's closing barrier)
-    for (int it = 0;; ++it) {
-        const int u = s_draw[it & 1];
+    for (;;) {
+        if (threadIdx.x == 0) s_unit = atomicAdd(cursor, 1);
+        __syncthreads();
+        const int u = s_unit;
+        __syncthreads();
         if (u >= n) break;
-        const int next = threadIdx.x == 0 ? atomicAdd(cursor, 1) : 0;
         const int gr = __ldg(queue + u);
         const int s = batch_segment(s_base, nseg, gr);
-        besc_row<Shape, kNum, T, KT>(s_segs[s], gr - s_base[s], sm, s_warp_sums, s_last, &s_sc, nnz_unused,
-                                     &s_draw[(it + 1) & 1], next);
+        besc_row<Shape, kNum, T, KT>(s_segs[s], gr - s_base[s], sm, s_warp_sums, s_last, &s_sc, nnz_unused);
     }
 }
 

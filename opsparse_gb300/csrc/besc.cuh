@@ -82,6 +82,7 @@ struct BescShape {
 };
 
 using BescE1 = BescShape<128, 8, 1024, 6, true>;        // E1 rows of more than kSplitNnz outputs
+using BescE1Sort = BescShape<128, 8, 1024, 6>;          // the same rows where B is wider than the window
 using BescE1Batch = BescShape<128, 8, 480, 7, true>;    // the batch's rows of 513 to 1,024 products
 using BescMid = BescShape<256, 16, 1280, 4>;            // E2 rows of at most 4,096 products
 using BescMidRank = BescShape<256, 16, 1280, 3, true>;  // the batch's rows of 1,025 to 4,096 products
@@ -612,15 +613,14 @@ __device__ __forceinline__ int besc_rank_scan_row(const SpgemmArgs<T> &g, int a0
 // expand, sort (or rank), then count (symbolic) or fold and write (numeric).  Symbolic and
 // one-pass calls write the row's count to c_rpt[r]; the count is also added to nnz_acc
 // (thread 0).  s_warp_sums (32 ints), s_last (32 keys) and sc are block-shared scratch;
-// sc must be reset on entry and is reset again on return.  Thread 0 stores publish_val to
-// *publish before the closing barrier (the caller's draw of its next row).  Every thread
-// of the CTA calls it; it ends with a barrier.  Rank shapes: when the row's column window (known from the
+// sc must be reset on entry and is reset again on return.  Every thread of the CTA calls
+// it; it ends with a barrier.  Rank shapes: when the row's column window (known from the
 // scan) spans fewer than kRankWinBits columns, the expansion also marks each product's
 // column in the window bitmap, so the rank path starts at its prefix sweep.
 template <typename Shape, bool kNum, typename T, typename KT>
 __device__ __forceinline__ void besc_row(const SpgemmArgs<T> &g, int r, const BescSmem<Shape, kNum, KT, T> &sm,
                                          int *s_warp_sums, KT *s_last, BescScratch *sc,
-                                         unsigned long long &nnz_acc, int *publish, int publish_val)
+                                         unsigned long long &nnz_acc)
 {
     constexpr int NT = Shape::kThreads;
     constexpr int kIdBits = kNum ? Shape::kIdBits : 0;
@@ -733,7 +733,6 @@ __device__ __forceinline__ void besc_row(const SpgemmArgs<T> &g, int r, const Be
             nnz_acc += (unsigned long long)total;
         }
     }
-    if (tid == 0) *publish = publish_val;
     __syncthreads();
     if (tid == 0) sc->reset();  // read by every thread before the barrier above
 }
@@ -746,26 +745,23 @@ __global__ void __launch_bounds__(Shape::kThreads, Shape::kMinBlocks) k_besc_row
     const int tid = threadIdx.x;
     __shared__ int s_warp_sums[32];
     __shared__ KT s_last[32];
-    __shared__ int s_draw[2];
+    __shared__ int s_row;
     __shared__ BescScratch s_sc;
     const BescSmem<Shape, kNum, KT, T> sm(smem_raw);
 
     const int count = *count_ptr;
     unsigned long long nnz_acc = 0;
-    if (tid == 0) {
-        s_sc.reset();
-        s_draw[0] = atomicAdd(cursor, 1);
-    }
+    if (tid == 0) s_sc.reset();
     sm.init();
-    __syncthreads();
-    // thread 0 draws the next row while the CTA works on the current one; two slots, so
-    // the draw is published by the row's closing barrier
-    for (int it = 0;; ++it) {
-        const int u = s_draw[it & 1];
-        if (u >= count) break;
-        const int next = tid == 0 ? atomicAdd(cursor, 1) : 0;
-        besc_row<Shape, kNum, T, KT>(g, __ldg(list + u), sm, s_warp_sums, s_last, &s_sc, nnz_acc,
-                                     &s_draw[(it + 1) & 1], next);
+    // rows are drawn one at a time when the CTA is free (lists are longest first, and a CTA
+    // takes only a few rows of a single call: drawing ahead would fix the schedule early)
+    for (;;) {
+        if (tid == 0) s_row = atomicAdd(cursor, 1);
+        __syncthreads();
+        const int it = s_row;
+        __syncthreads();
+        if (it >= count) break;
+        besc_row<Shape, kNum, T, KT>(g, __ldg(list + it), sm, s_warp_sums, s_last, &s_sc, nnz_acc);
     }
     if (tid == 0 && nnz_acc) atomicAdd(&g.info->total_nnz, nnz_acc);
 }

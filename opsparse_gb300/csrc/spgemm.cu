@@ -72,6 +72,17 @@ void launch_besc(const SpgemmArgs<T> &g, const int *list, const int *count_ptr, 
     }
 }
 
+// The E1 expand rows' numeric kernel: the rank shape where B has at most kRankWinBits
+// columns (every row fits the window), else the sort-only shape, whose smaller shared
+// memory keeps one more CTA per SM for rows that could not take the rank path.
+template <typename T>
+void launch_besc_e1(const SpgemmArgs<T> &g, const int *list, const int *count_ptr, int *cursor, int grid,
+                    cudaStream_t s)
+{
+    if (g.N <= kRankWinBits) launch_besc<BescE1, true, T>(g, list, count_ptr, cursor, grid, s);
+    else launch_besc<BescE1Sort, true, T>(g, list, count_ptr, cursor, grid, s);
+}
+
 template <typename T>
 void set_smem_attrs()
 {
@@ -86,6 +97,7 @@ void set_smem_attrs()
     cudaFuncSetAttribute(k_warp_rows<false, T, 2 * kEsc1FlopMax>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)warp_rows_smem<false, T, 2 * kEsc1FlopMax>());
     set_besc_attrs<BescE1, T>();
+    set_besc_attrs<BescE1Sort, T>();
     set_besc_attrs<BescMid, T>();
     cudaFuncSetAttribute(k_wsort_rows<4, true, T, unsigned>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)WsortShape<4>::smem<true, T, unsigned>());
@@ -248,8 +260,8 @@ int launch_staged_class(ops_handle_s *h, const GA &gs, int c, const int *list, i
             ++h->launches;
             OPS_CUDA(h, cudaEventRecord(h->ev_x_fork[0], s));
             OPS_CUDA(h, cudaStreamWaitEvent(h->side_x[0], h->ev_x_fork[0], 0));
-            launch_besc<BescE1, true, T>(g, one_large, &h->info->split1[2], &h->info->next[0][c],
-                                         std::min(n, sms * 8), h->side_x[0]);
+            launch_besc_e1<T>(g, one_large, &h->info->split1[2], &h->info->next[0][c], std::min(n, sms * 8),
+                              h->side_x[0]);
             OPS_CUDA(h, cudaGetLastError());
             ++h->launches;
             SpgemmArgs<double> gc{};
@@ -480,8 +492,7 @@ int launch_classes(ops_handle_s *h, const SpgemmArgs<T> &g, cudaStream_t st)
                 ++h->launches;
                 cudaStream_t sx = fork_x(0, s);
                 if (!sx) return fail(h, OPS_CUDA_ERROR, "stream fork failed");
-                launch_besc<BescE1, true, T>(g, esc_list, &h->info->split[2], &h->info->next[1][c],
-                                             std::min(n, sms * 8), sx);
+                launch_besc_e1<T>(g, esc_list, &h->info->split[2], &h->info->next[1][c], std::min(n, sms * 8), sx);
                 OPS_CUDA(h, cudaGetLastError());
                 ++h->launches;
                 if (!join_x(0, s)) return fail(h, OPS_CUDA_ERROR, "stream join failed");

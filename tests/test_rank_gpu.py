@@ -4,7 +4,7 @@ outputs whose columns span fewer than 65,536 columns).
 Rows are built to reach each branch: products in distinct columns (rank, no late
 product), a few products in repeated columns (re-fold of 20, 50 and 100 late products:
 the one-, two- and four-key-per-lane sorts of the late list), many repeated columns (more
-than 128 late products: the sort), and columns spread wider than the window (the sort,
+than 128 late products: the sort), and a B wider than the window (the sort-only kernel,
 not counted).  Through the two-pass and the one-pass call, FP64 and FP32: results
 bit-identical to the oracle, and the rows counted on each path.
 """
@@ -41,12 +41,19 @@ def _row_b_rows(rng, kind, span):
     raise ValueError(kind)
 
 
-def rank_case(seed=5):
-    """A: 7 groups of 40 rows; row i owns B rows [24 i, 24 i + 24).  The last group's
-    columns spread over 200,000 columns (wider than the window)."""
+def rank_case(seed=5, wide=False):
+    """A: 40 rows per group; row i owns B rows [24 i, 24 i + 24).  Narrow groups (B of
+    65,536 columns, so every row fits the window): products in distinct columns (80 rows),
+    20, 50 and 100 late products (40 rows each) and crowded columns (40 rows).  wide=True:
+    40 rows of distinct columns spread over 200,000 columns (B wider than the window: the
+    sort-only shape)."""
     rng = np.random.default_rng(seed)
-    kinds = [("distinct", 60000), ("late20", 60000), ("late50", 50000), ("late100", 65536), ("crowded", 30000),
-             ("distinct", 2000), ("distinct", 200000)]
+    if wide:
+        kinds, ncols = [("distinct", 200000)], 200000
+    else:
+        kinds = [("distinct", 60000), ("late20", 60000), ("late50", 50000), ("late100", 65536), ("crowded", 30000),
+                 ("distinct", 2000)]
+        ncols = 65536
     b_rows = []
     for kind, span in kinds:
         for _ in range(40):
@@ -58,14 +65,15 @@ def rank_case(seed=5):
     b_rpt = np.concatenate([[0], np.cumsum([len(r) for r in b_rows])]).astype(np.int32)
     b_col = np.concatenate(b_rows).astype(np.int32)
     b_val = rng.standard_normal(len(b_col))
-    return (a_rpt, a_col, a_val), (b_rpt, b_col, b_val), 200000
+    return (a_rpt, a_col, a_val), (b_rpt, b_col, b_val), ncols
 
 
+@pytest.mark.parametrize("wide", [False, True], ids=["window", "wide"])
 @pytest.mark.parametrize("oneshot", [False, True], ids=["two_phase", "one_pass"])
 @pytest.mark.parametrize("dtype", ["f64", "f32"])
-def test_rank_path_branches(cuda, dtype, oneshot):
+def test_rank_path_branches(cuda, dtype, oneshot, wide):
     torch = cuda
-    a, b, ncols = rank_case()
+    a, b, ncols = rank_case(wide=wide)
     tdt = torch.float64 if dtype == "f64" else torch.float32
     npdt = np.float64 if dtype == "f64" else np.float32
     a = (a[0], a[1], a[2].astype(npdt))
@@ -83,6 +91,9 @@ def test_rank_path_branches(cuda, dtype, oneshot):
     assert np.array_equal(col, ocol)
     bits = np.uint64 if dtype == "f64" else np.uint32
     assert np.array_equal(val.view(bits), oval.view(bits))
-    # 80 rows on the rank path without late products, 120 re-folded, 40 sorted (the
-    # widely spread rows are not counted)
-    assert sub["rank"] == 80 and sub["rank_refold"] == 120 and sub["rank_sorted"] == 40, sub
+    assert sub["e1_esc"] == len(rpt) - 1, sub  # every row is an expand row
+    if wide:
+        assert sub["rank"] == 0 and sub["rank_refold"] == 0 and sub["rank_sorted"] == 0, sub
+    else:
+        # 80 rows without late products, 120 re-folded, 40 sorted
+        assert sub["rank"] == 80 and sub["rank_refold"] == 120 and sub["rank_sorted"] == 40, sub
