@@ -50,6 +50,15 @@ constexpr int kEsc1FlopMax = 1024;
 constexpr int kEsc1AMax = 1024;
 constexpr int kEsc2FlopMax = 13312;
 constexpr int kEsc2AMax = 2560;
+// Entries of more than kBlockFoldMin products fold in kFoldBlocks consecutive blocks of
+// ceil(m / kFoldBlocks) products each (each block the plain ascending-j fold from zero),
+// the block states merged in block order (Acc::merge).  An entry has at most as many
+// products as A's row has entries (a B row holds a column once), so only D rows, whose A
+// rows may exceed every other class's limit, can have such entries.
+constexpr int kBlockFoldMin = 2560;
+constexpr int kFoldBlocks = 32;
+static_assert(kBlockFoldMin >= kEsc2AMax && kBlockFoldMin >= kEsc1AMax && kBlockFoldMin >= 128,
+              "entries of more than kBlockFoldMin products occur only in D rows");
 // E1 rows computed in the counting phase of a one-pass call: by warp sort up to this many
 // products, by CTA expand/sort/compress above; column-window rows (below) keep two passes
 constexpr int kE1OnePassFlopMax = 512;
@@ -180,6 +189,9 @@ struct Acc<double> {
     __device__ __forceinline__ static S zero() { return 0.0; }
     __device__ __forceinline__ static S step(S s, double a, double b) { return __fma_rn(a, b, s); }
     __device__ __forceinline__ static double fin(S s) { return s; }
+    // states of two consecutive blocks of an entry's products
+    __device__ __forceinline__ static S merge(S u, S v) { return __dadd_rn(u, v); }
+    __device__ __forceinline__ static S shfl(S v, int src) { return __shfl_sync(0xffffffffu, v, src); }
 };
 
 template <>
@@ -196,6 +208,19 @@ struct Acc<float> {
         return make_float2(s, __fadd_rn(st.y, __fadd_rn(q, r)));
     }
     __device__ __forceinline__ static float fin(S st) { return __fadd_rn(st.x, st.y); }
+    // states of two consecutive blocks: TwoSum of the sums, the compensations added, then
+    // the TwoSum error
+    __device__ __forceinline__ static S merge(S u, S v)
+    {
+        const float s = __fadd_rn(u.x, v.x);
+        const float z = __fsub_rn(s, u.x);
+        const float q = __fadd_rn(__fsub_rn(u.x, __fsub_rn(s, z)), __fsub_rn(v.x, z));
+        return make_float2(s, __fadd_rn(__fadd_rn(u.y, v.y), q));
+    }
+    __device__ __forceinline__ static S shfl(S v, int src)
+    {
+        return make_float2(__shfl_sync(0xffffffffu, v.x, src), __shfl_sync(0xffffffffu, v.y, src));
+    }
 };
 
 template <typename T>
@@ -221,6 +246,30 @@ __device__ __forceinline__ typename Acc<T>::S fold_group(typename Acc<T>::S s, u
         }
     }
     return s;
+}
+
+// fold_group for an entry folded in blocks (c = products per block, 0 for a plain entry):
+// cur is the current block's state, tot the merge of the finished blocks, pos the number of
+// the entry's products folded so far.
+template <typename T>
+__device__ __forceinline__ void fold_group_blocked(typename Acc<T>::S &cur, typename Acc<T>::S &tot, int &pos, int c,
+                                                   unsigned members, T a, T b)
+{
+    const int lane = lane_id();
+    while (__any_sync(kFull, members != 0u)) {
+        const int src = members ? (__ffs(members) - 1) : lane;
+        const T am = shfl(a, src);
+        const T bm = shfl(b, src);
+        if (members) {
+            if (c && pos && pos % c == 0) {  // the first product of a new block
+                tot = pos == c ? cur : Acc<T>::merge(tot, cur);
+                cur = Acc<T>::zero();
+            }
+            cur = Acc<T>::step(cur, am, bm);
+            ++pos;
+            members &= members - 1u;
+        }
+    }
 }
 
 // ----------------------------------------------------------------------------------

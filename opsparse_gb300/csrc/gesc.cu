@@ -15,9 +15,11 @@
 //      record where each run starts, and fold each run with one FMA per product — by
 //      one thread for runs of at most 32 products, by a warp for longer runs (the lanes
 //      gather the operands of the next two batches of 32 while lane 0 folds the current
-//      32 from shared memory; a run is a chain of dependent FMAs and cannot be split, and
-//      a dependent FP64 FMA costs about 64 cycles on GB300, so the longest run bounds
-//      the phase).  C entry h of
+//      32 from shared memory: a run is a chain of dependent FMAs, and a dependent FP64
+//      FMA costs about 64 cycles on GB300).  Runs of more than kBlockFoldMin products
+//      fold in kFoldBlocks blocks, lane b the b-th, merged in lane order by lane 0 — the
+//      fixed blocked order the oracle uses for such entries — so the longest chain is
+//      at most kBlockFoldMin FMAs.  C entry h of
 //      D row d goes to row_ptr[row] + h - (heads of the earlier D rows).
 #include <cub/cub.cuh>
 
@@ -301,6 +303,43 @@ __global__ void __launch_bounds__(kThreads) k_d_fold_long(const KT *__restrict__
                 b = __ldg(bval + (int)(v & 0xffffffffu));
             }
         };
+        if (t1 - t0 > (unsigned)kBlockFoldMin) {
+            // blocked entry: lane b folds products [t0 + b c, t0 + (b + 1) c), eight
+            // products' operands in flight; lane 0 merges the lanes' states in order
+            static_assert(kFoldBlocks == 32, "a lane per block");
+            const unsigned c = (t1 - t0 + kFoldBlocks - 1) / kFoldBlocks;
+            const unsigned q0 = t0 + (unsigned)lane * c;
+            const unsigned q1 = min(t1, q0 + c);
+            typename AccT::S s = AccT::zero();
+            for (unsigned q = q0; q < q1; q += 8) {
+                T a8[8], b8[8];
+#pragma unroll
+                for (int u = 0; u < 8; ++u) {
+                    a8[u] = T(0);
+                    b8[u] = T(0);
+                    if (q + u < q1) {
+                        const unsigned long long v = vals[q + u];
+                        a8[u] = __ldg(aval + (int)(v >> 32));
+                        b8[u] = __ldg(bval + (int)(v & 0xffffffffu));
+                    }
+                }
+#pragma unroll
+                for (int u = 0; u < 8; ++u)
+                    if (q + u < q1) s = AccT::step(s, a8[u], b8[u]);
+            }
+            typename AccT::S tot = s;
+            for (int b = 1; b < kFoldBlocks; ++b) {
+                const typename AccT::S o = AccT::shfl(s, b);
+                if (lane == 0) tot = AccT::merge(tot, o);
+            }
+            if (lane == 0) {
+                const KT k0 = keys[t0];
+                d_write<T>(h, (int)(k0 >> cb), (int)(k0 & ((KT(1) << cb) - 1)), tot, hcum, list, c_rpt, soff, c_col,
+                           c_val, flags);
+            }
+            __syncwarp();
+            continue;
+        }
         // two batches in flight ahead of the fold: a batch's gather (two dependent loads)
         // takes about as long as 32 dependent FP64 FMAs (~64 cycles each on this GPU)
         T na, nb, na2, nb2;

@@ -1165,7 +1165,10 @@ __device__ __forceinline__ void block_products_ordered(int a0, int a1, const Spg
 // it touched).  Symbolic: atomicOr on the bitmap counts first insertions.  Numeric:
 // ordered CTA-chunk walk into vals[col]; then the bitmap words between the row's
 // smallest and largest column are split into contiguous per-thread pieces, counted,
-// scanned and walked in order, which emits ascending columns with no sort.
+// scanned and walked in order, which emits ascending columns with no sort.  Rows of more
+// than kBlockFoldMin A entries first count each column's products (cnt); the walk folds
+// an entry of more than kBlockFoldMin products in blocks (vals = the current block,
+// tot = the merged earlier blocks, pos = products folded), as every other path does.
 // ==================================================================================
 constexpr int kDenseRowsThreads = 512;
 
@@ -1173,6 +1176,9 @@ template <typename T>
 struct DenseScratch {
     typename Acc<T>::S *vals;  // gridDim.x * N
     unsigned *bits;            // gridDim.x * words
+    typename Acc<T>::S *tot;   // gridDim.x * N: merged earlier blocks of a blocked entry
+    int *cnt;                  // gridDim.x * N: products per column (rows of long entries)
+    int *pos;                  // gridDim.x * N: products of a blocked entry folded so far
     int words;                 // ceil(N / 32)
 };
 
@@ -1191,6 +1197,9 @@ __global__ void __launch_bounds__(kDenseRowsThreads) k_dense_rows(SpgemmArgs<T> 
     constexpr int kWarps = NT / 32;
     S *vals = ds.vals + (size_t)blockIdx.x * (size_t)g.N;
     unsigned *bits = ds.bits + (size_t)blockIdx.x * (size_t)ds.words;
+    S *totc = ds.tot + (size_t)blockIdx.x * (size_t)g.N;
+    int *cntc = ds.cnt + (size_t)blockIdx.x * (size_t)g.N;
+    int *posc = ds.pos + (size_t)blockIdx.x * (size_t)g.N;
     const unsigned N = (unsigned)g.N;
     unsigned long long nnz_acc = 0;
 
@@ -1215,6 +1224,16 @@ __global__ void __launch_bounds__(kDenseRowsThreads) k_dense_rows(SpgemmArgs<T> 
                 }
             });
         } else {
+            const bool long_row = a1 - a0 > kBlockFoldMin;  // may hold entries folded in blocks
+            if (long_row) {
+                warp_products<false, T>(a0 + warp * 32, a1, NT, g.acol, g.aval, g.brpt, [&](bool valid, int k, T, int) {
+                    if (valid) {
+                        const int col = __ldg(g.bcol + k);
+                        if ((unsigned)col < N) atomicAdd(cntc + col, 1);
+                    }
+                });
+                __syncthreads();
+            }
             block_products_ordered<NT, T>(
                 a0, a1, g, cs,
                 [&](bool valid, int col, bool leader) -> int {
@@ -1226,9 +1245,31 @@ __global__ void __launch_bounds__(kDenseRowsThreads) k_dense_rows(SpgemmArgs<T> 
                     return col;
                 },
                 [&](int slot, unsigned members, T a, T b) {
-                    S s = slot >= 0 ? vals[slot] : AccT::zero();
-                    s = fold_group<T>(s, members, a, b);
-                    if (slot >= 0) vals[slot] = s;
+                    if (!long_row) {
+                        S s = slot >= 0 ? vals[slot] : AccT::zero();
+                        s = fold_group<T>(s, members, a, b);
+                        if (slot >= 0) vals[slot] = s;
+                        return;
+                    }
+                    S cur = AccT::zero(), acc_tot = AccT::zero();
+                    int pos = 0, c = 0;
+                    if (slot >= 0) {
+                        cur = vals[slot];
+                        const int m = cntc[slot];
+                        if (m > kBlockFoldMin) {
+                            c = (m + kFoldBlocks - 1) / kFoldBlocks;
+                            pos = posc[slot];
+                            acc_tot = totc[slot];
+                        }
+                    }
+                    fold_group_blocked<T>(cur, acc_tot, pos, c, members, a, b);
+                    if (slot >= 0) {
+                        vals[slot] = cur;
+                        if (c) {
+                            posc[slot] = pos;
+                            totc[slot] = acc_tot;
+                        }
+                    }
                 });
         }
         // Block reduction of (cnt, kmin, kmax).
@@ -1278,6 +1319,7 @@ __global__ void __launch_bounds__(kDenseRowsThreads) k_dense_rows(SpgemmArgs<T> 
             const int incl = block_inclusive_scan(mine, cs.warp_sums, &total);
             if (tid == 0 && total != n_expect) atomicOr(&g.info->flags, kErrCountMismatch);
             int pos = incl - mine;
+            const bool long_row = a1 - a0 > kBlockFoldMin;
             for (int w = wb; w < we; ++w) {
                 unsigned word = bits[w0 + w];
                 if (word) bits[w0 + w] = 0u;
@@ -1285,9 +1327,18 @@ __global__ void __launch_bounds__(kDenseRowsThreads) k_dense_rows(SpgemmArgs<T> 
                     const int b = __ffs(word) - 1;
                     word &= word - 1u;
                     const int col = ((w0 + w) << 5) + b;
+                    S v = vals[col];
+                    if (long_row) {
+                        if (cntc[col] > kBlockFoldMin) {  // the last block merged into the others
+                            v = AccT::merge(totc[col], v);
+                            totc[col] = AccT::zero();
+                            posc[col] = 0;
+                        }
+                        cntc[col] = 0;
+                    }
                     if (pos < n_expect) {
                         g.c_col[off + pos] = col;
-                        g.c_val[off + pos] = AccT::fin(vals[col]);
+                        g.c_val[off + pos] = AccT::fin(v);
                     }
                     vals[col] = AccT::zero();
                     ++pos;

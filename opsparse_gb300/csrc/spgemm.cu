@@ -17,6 +17,7 @@
 #include <cub/cub.cuh>
 
 #include <algorithm>
+#include <array>
 #include <cstdio>
 #include <cstring>
 #include <new>
@@ -141,15 +142,31 @@ int ensure_ws(ops_handle_s *h, int M, cudaStream_t st)
     return OPS_OK;
 }
 
-// Dense-row scratch: per CTA, N accumulator slots (8 bytes) and ceil(N/32) bitmap words.
+// Region ends of the dense-row scratch for `ctas` CTAs: [vals | bits | tot | cnt | pos],
+// each region 256-byte aligned.
+std::array<size_t, 5> dense_offsets(int N, int ctas)
+{
+    const size_t n = (size_t)N * (size_t)ctas, words = (size_t)(N + 31) / 32 * (size_t)ctas;
+    std::array<size_t, 5> o{};
+    o[0] = align_up(n * 8, 256);
+    o[1] = o[0] + align_up(words * 4, 256);
+    o[2] = o[1] + align_up(n * 8, 256);
+    o[3] = o[2] + align_up(n * 4, 256);
+    o[4] = o[3] + align_up(n * 4, 256);
+    return o;
+}
+
+// Dense-row scratch: per CTA, N accumulator slots (8 bytes), ceil(N/32) bitmap words, and
+// for entries folded in blocks N merged-block slots (8 bytes), N product counts and N
+// positions (4 bytes each).
 int ensure_dense(ops_handle_s *h, int N, int rows, cudaStream_t st)
 {
     const size_t words = (size_t)(N + 31) / 32;
-    const size_t per_cta = (size_t)N * 8 + words * 4;
+    const size_t per_cta = (size_t)N * 24 + words * 4;
     int ctas = std::min(rows, 2 * h->num_sms);
     const size_t by_budget = per_cta ? h->dense_budget / per_cta : (size_t)ctas;
     ctas = (int)std::max<size_t>(1, std::min<size_t>((size_t)ctas, by_budget));
-    const size_t need = align_up(per_cta * (size_t)ctas, 256) + 256;
+    const size_t need = dense_offsets(N, ctas)[4] + 256;
     if (need > h->dense_bytes) {
         if (h->dense) {
             OPS_CUDA(h, cudaFreeAsync(h->dense, st));
@@ -169,10 +186,14 @@ int ensure_dense(ops_handle_s *h, int N, int rows, cudaStream_t st)
 template <typename T>
 DenseScratch<T> dense_view(ops_handle_s *h, int N)
 {
+    const std::array<size_t, 5> o = dense_offsets(N, h->dense_ctas);
     DenseScratch<T> d;
     d.words = (N + 31) / 32;
     d.vals = reinterpret_cast<typename Acc<T>::S *>(h->dense);
-    d.bits = reinterpret_cast<unsigned *>(h->dense + align_up((size_t)N * 8 * (size_t)h->dense_ctas, 256));
+    d.bits = reinterpret_cast<unsigned *>(h->dense + o[0]);
+    d.tot = reinterpret_cast<typename Acc<T>::S *>(h->dense + o[1]);
+    d.cnt = reinterpret_cast<int *>(h->dense + o[2]);
+    d.pos = reinterpret_cast<int *>(h->dense + o[3]);
     return d;
 }
 

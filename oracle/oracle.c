@@ -17,9 +17,14 @@
  *    cancel to 0.0 are kept, numeric.cuh:183-192), with ascending columns per row
  *    (the rank sort of numeric.cuh:196-204).  Each value is accumulated in a FIXED order:
  *    contributions in ascending j (A's column order), each folded in with one fused
- *    multiply-add, c = fma(a_ij, b_jk, c), starting from +0.0.  The reference itself
- *    adds in a run-dependent order (atomicAdd), so its values agree with this only to
- *    rounding; the GB300 library uses this exact order and is compared bit-for-bit.
+ *    multiply-add, c = fma(a_ij, b_jk, c), starting from +0.0.  An entry with more than
+ *    ORC_BLOCK_FOLD_MIN (2,560) contributions — possible only where A's row has more
+ *    entries than that, since a B row holds a column once — is folded in ORC_BLOCKS (32)
+ *    consecutive blocks of c = ceil(m / 32) of its m contributions, each block the same
+ *    fma chain from +0.0, and the block sums added in block order,
+ *    ((s_0 + s_1) + s_2) + ...  The reference itself adds in a run-dependent order
+ *    (atomicAdd), so its values agree with this only to rounding; the GB300 library uses
+ *    this exact order and is compared bit-for-bit.
  *  - orc_spgemm_f32: the same structure for FP32 values, each entry accumulated with the
  *    compensated dot product "Dot2" of Ogita, Rump and Oishi (Accurate Sum and Dot
  *    Product, SIAM J. Sci. Comput. 26(6), 2005): TwoProduct via fmaf, TwoSum, and a
@@ -28,7 +33,8 @@
  *    dA_ij = sum_k B_jk dC_ik and dB_jk = sum_i A_ij dC_ik (no reference counterpart).
  *  - orc_omp_symbolic / orc_omp_numeric_f64: OpenMP row-wise Gustavson hash SpGEMM (two
  *    phases, per-thread open-addressing tables), the timed CPU baseline.  Same summation order as
- *    orc_spgemm_f64, so its output is bit-identical to it.
+ *    orc_spgemm_f64 (plain ascending j for every entry), so its output is bit-identical to
+ *    it wherever no entry has more than ORC_BLOCK_FOLD_MIN contributions.
  *
  * Pinning: flop counts, structure and values are checked against the reference's own
  * kernels and host compute_flop, compiled from its sources and run on the CPU
@@ -112,6 +118,66 @@ static int cmp_i32(const void *a, const void *b)
     return (x > y) - (x < y);
 }
 
+#define ORC_BLOCK_FOLD_MIN 2560 /* entries with more contributions fold in blocks */
+#define ORC_BLOCKS 32
+
+/* Block of contribution t (0-based) of an entry with m contributions. */
+static inline int64_t orc_block_of(int64_t t, int64_t m)
+{
+    return t / ((m + ORC_BLOCKS - 1) / ORC_BLOCKS);
+}
+
+/* Per-thread scratch of the long-entry rows: contributions and block slot per column. */
+typedef struct {
+    int32_t *cnt, *slot, *pos;
+} orc_long_scratch;
+
+static orc_long_scratch orc_long_alloc(int32_t N)
+{
+    orc_long_scratch ls;
+    const size_t n = (size_t)(N > 0 ? N : 1);
+    ls.cnt = (int32_t *)malloc(n * sizeof(int32_t));
+    ls.slot = (int32_t *)malloc(n * sizeof(int32_t));
+    ls.pos = (int32_t *)malloc(n * sizeof(int32_t));
+    return ls;
+}
+
+static void orc_long_free(orc_long_scratch *ls)
+{
+    free(ls->cnt);
+    free(ls->slot);
+    free(ls->pos);
+}
+
+/* Distinct columns of row i into cols (first-touch order) with their contribution counts;
+ * entries with more than ORC_BLOCK_FOLD_MIN get consecutive slots.  Returns the number of
+ * distinct columns; *nlong receives the number of slots. */
+static int64_t orc_long_count(int32_t i, const int32_t *arpt, const int32_t *acol, const int32_t *brpt,
+                              const int32_t *bcol, int32_t *mark, int32_t *cols, orc_long_scratch *ls,
+                              int64_t *nlong)
+{
+    int64_t n = 0, nl = 0;
+    for (int32_t p = arpt[i]; p < arpt[i + 1]; p++) {
+        const int32_t j = acol[p];
+        for (int32_t q = brpt[j]; q < brpt[j + 1]; q++) {
+            const int32_t k = bcol[q];
+            if (mark[k] != i) {
+                mark[k] = i;
+                ls->cnt[k] = 0;
+                cols[n++] = k;
+            }
+            ls->cnt[k]++;
+        }
+    }
+    for (int64_t t = 0; t < n; t++) {
+        const int32_t k = cols[t];
+        ls->pos[k] = 0;
+        ls->slot[k] = ls->cnt[k] > ORC_BLOCK_FOLD_MIN ? (int32_t)nl++ : -1;
+    }
+    *nlong = nl;
+    return n;
+}
+
 /* Fills ccol/cval given crpt from orc_symbolic.  Dense accumulator per thread; the
  * first touch of column k starts its sum at +0.0 and every contribution is folded in
  * with fma() in ascending j. */
@@ -123,22 +189,53 @@ void orc_spgemm_f64(int32_t M, int32_t N, const int32_t *arpt, const int32_t *ac
     {
         int32_t *mark = (int32_t *)malloc((size_t)(N > 0 ? N : 1) * sizeof(int32_t));
         double *acc = (double *)malloc((size_t)(N > 0 ? N : 1) * sizeof(double));
+        orc_long_scratch ls = orc_long_alloc(N);
         for (int32_t k = 0; k < N; k++) mark[k] = -1;
 #pragma omp for schedule(dynamic, 256)
         for (int32_t i = 0; i < M; i++) {
             int64_t n = 0;
             int32_t *cols = ccol + crpt[i];
-            for (int32_t p = arpt[i]; p < arpt[i + 1]; p++) {
-                const int32_t j = acol[p];
-                const double a = aval[p];
-                for (int32_t q = brpt[j]; q < brpt[j + 1]; q++) {
-                    const int32_t k = bcol[q];
-                    if (mark[k] != i) {
-                        mark[k] = i;
-                        acc[k] = 0.0;
-                        cols[n++] = k;
+            if (arpt[i + 1] - arpt[i] > ORC_BLOCK_FOLD_MIN) {
+                /* a row that may hold long entries: count first, then fold */
+                int64_t nl = 0;
+                n = orc_long_count(i, arpt, acol, brpt, bcol, mark, cols, &ls, &nl);
+                double *part = (double *)calloc((size_t)(nl > 0 ? nl : 1) * ORC_BLOCKS, sizeof(double));
+                for (int64_t t = 0; t < n; t++) acc[cols[t]] = 0.0;
+                for (int32_t p = arpt[i]; p < arpt[i + 1]; p++) {
+                    const int32_t j = acol[p];
+                    const double a = aval[p];
+                    for (int32_t q = brpt[j]; q < brpt[j + 1]; q++) {
+                        const int32_t k = bcol[q];
+                        if (ls.slot[k] >= 0) {
+                            double *pb = part + (size_t)ls.slot[k] * ORC_BLOCKS + orc_block_of(ls.pos[k]++, ls.cnt[k]);
+                            *pb = fma(a, bval[q], *pb);
+                        } else {
+                            acc[k] = fma(a, bval[q], acc[k]);
+                        }
                     }
-                    acc[k] = fma(a, bval[q], acc[k]);
+                }
+                for (int64_t t = 0; t < n; t++) {
+                    const int32_t k = cols[t];
+                    if (ls.slot[k] < 0) continue;
+                    const double *pb = part + (size_t)ls.slot[k] * ORC_BLOCKS;
+                    double s = pb[0];
+                    for (int b = 1; b < ORC_BLOCKS; b++) s = s + pb[b];
+                    acc[k] = s;
+                }
+                free(part);
+            } else {
+                for (int32_t p = arpt[i]; p < arpt[i + 1]; p++) {
+                    const int32_t j = acol[p];
+                    const double a = aval[p];
+                    for (int32_t q = brpt[j]; q < brpt[j + 1]; q++) {
+                        const int32_t k = bcol[q];
+                        if (mark[k] != i) {
+                            mark[k] = i;
+                            acc[k] = 0.0;
+                            cols[n++] = k;
+                        }
+                        acc[k] = fma(a, bval[q], acc[k]);
+                    }
                 }
             }
             qsort(cols, (size_t)n, sizeof(int32_t), cmp_i32);
@@ -146,6 +243,7 @@ void orc_spgemm_f64(int32_t M, int32_t N, const int32_t *arpt, const int32_t *ac
         }
         free(mark);
         free(acc);
+        orc_long_free(&ls);
     }
 }
 
@@ -168,6 +266,19 @@ static inline dot2_t dot2_step(dot2_t st, float a, float b)
     return out;
 }
 
+/* Two Dot2 states of consecutive blocks combined: TwoSum of the sums, the compensations
+ * added, then the TwoSum error. */
+static inline dot2_t dot2_merge(dot2_t u, dot2_t v)
+{
+    const float s = u.s + v.s;
+    const float z = s - u.s;
+    const float q = (u.s - (s - z)) + (v.s - z);
+    dot2_t out;
+    out.s = s;
+    out.c = (u.c + v.c) + q;
+    return out;
+}
+
 void orc_spgemm_f32(int32_t M, int32_t N, const int32_t *arpt, const int32_t *acol, const float *aval,
                     const int32_t *brpt, const int32_t *bcol, const float *bval, const int64_t *crpt, int32_t *ccol,
                     float *cval)
@@ -176,23 +287,56 @@ void orc_spgemm_f32(int32_t M, int32_t N, const int32_t *arpt, const int32_t *ac
     {
         int32_t *mark = (int32_t *)malloc((size_t)(N > 0 ? N : 1) * sizeof(int32_t));
         dot2_t *acc = (dot2_t *)malloc((size_t)(N > 0 ? N : 1) * sizeof(dot2_t));
+        orc_long_scratch ls = orc_long_alloc(N);
         for (int32_t k = 0; k < N; k++) mark[k] = -1;
 #pragma omp for schedule(dynamic, 256)
         for (int32_t i = 0; i < M; i++) {
             int64_t n = 0;
             int32_t *cols = ccol + crpt[i];
-            for (int32_t p = arpt[i]; p < arpt[i + 1]; p++) {
-                const int32_t j = acol[p];
-                const float a = aval[p];
-                for (int32_t q = brpt[j]; q < brpt[j + 1]; q++) {
-                    const int32_t k = bcol[q];
-                    if (mark[k] != i) {
-                        mark[k] = i;
-                        acc[k].s = 0.0f;
-                        acc[k].c = 0.0f;
-                        cols[n++] = k;
+            if (arpt[i + 1] - arpt[i] > ORC_BLOCK_FOLD_MIN) {
+                int64_t nl = 0;
+                n = orc_long_count(i, arpt, acol, brpt, bcol, mark, cols, &ls, &nl);
+                dot2_t *part = (dot2_t *)calloc((size_t)(nl > 0 ? nl : 1) * ORC_BLOCKS, sizeof(dot2_t));
+                for (int64_t t = 0; t < n; t++) {
+                    acc[cols[t]].s = 0.0f;
+                    acc[cols[t]].c = 0.0f;
+                }
+                for (int32_t p = arpt[i]; p < arpt[i + 1]; p++) {
+                    const int32_t j = acol[p];
+                    const float a = aval[p];
+                    for (int32_t q = brpt[j]; q < brpt[j + 1]; q++) {
+                        const int32_t k = bcol[q];
+                        if (ls.slot[k] >= 0) {
+                            dot2_t *pb = part + (size_t)ls.slot[k] * ORC_BLOCKS + orc_block_of(ls.pos[k]++, ls.cnt[k]);
+                            *pb = dot2_step(*pb, a, bval[q]);
+                        } else {
+                            acc[k] = dot2_step(acc[k], a, bval[q]);
+                        }
                     }
-                    acc[k] = dot2_step(acc[k], a, bval[q]);
+                }
+                for (int64_t t = 0; t < n; t++) {
+                    const int32_t k = cols[t];
+                    if (ls.slot[k] < 0) continue;
+                    const dot2_t *pb = part + (size_t)ls.slot[k] * ORC_BLOCKS;
+                    dot2_t st = pb[0];
+                    for (int b = 1; b < ORC_BLOCKS; b++) st = dot2_merge(st, pb[b]);
+                    acc[k] = st;
+                }
+                free(part);
+            } else {
+                for (int32_t p = arpt[i]; p < arpt[i + 1]; p++) {
+                    const int32_t j = acol[p];
+                    const float a = aval[p];
+                    for (int32_t q = brpt[j]; q < brpt[j + 1]; q++) {
+                        const int32_t k = bcol[q];
+                        if (mark[k] != i) {
+                            mark[k] = i;
+                            acc[k].s = 0.0f;
+                            acc[k].c = 0.0f;
+                            cols[n++] = k;
+                        }
+                        acc[k] = dot2_step(acc[k], a, bval[q]);
+                    }
                 }
             }
             qsort(cols, (size_t)n, sizeof(int32_t), cmp_i32);
@@ -200,6 +344,7 @@ void orc_spgemm_f32(int32_t M, int32_t N, const int32_t *arpt, const int32_t *ac
         }
         free(mark);
         free(acc);
+        orc_long_free(&ls);
     }
 }
 

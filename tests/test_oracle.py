@@ -131,3 +131,81 @@ def test_backward_matches_dense_gradient():
     rows_b = np.repeat(np.arange(40), np.diff(B.indptr))
     assert np.allclose(da, dA[rows_a, A.indices], rtol=1e-12, atol=1e-12)
     assert np.allclose(db, dB[rows_b, B.indices], rtol=1e-12, atol=1e-12)
+
+
+def _long_entry_case(m=5000, seed=31):
+    """One A row of m entries, all 1.0, over B rows that each hold column 0 and one other
+    column: C[0, 0] has m contributions (folded in blocks), the others one each."""
+    rng = np.random.default_rng(seed)
+    arpt = np.array([0, m], dtype=np.int32)
+    acol = np.arange(m, dtype=np.int32)
+    aval = np.ones(m)
+    brpt = np.arange(0, 2 * m + 1, 2, dtype=np.int32)
+    bcol = np.stack([np.zeros(m, dtype=np.int32), 1 + np.arange(m, dtype=np.int32)], axis=1).ravel()
+    bval = rng.standard_normal(2 * m)
+    return (arpt, acol, aval), (brpt, bcol, bval), m + 1
+
+
+def test_oracle_blocked_long_entry_f64():
+    """Entries of more than 2,560 contributions fold in 32 consecutive blocks of ceil(m/32),
+    each from +0.0 in ascending j, the block sums added in order (with a = 1.0 every fma is
+    an exact addition, so Python floats restate it)."""
+    a, b, n = _long_entry_case()
+    _, col, val = oracle.spgemm(*a, *b, n)
+    terms = [float(x) for x in b[2][0::2]]  # B values of column 0, ascending j
+    c = (len(terms) + 31) // 32
+    parts = []
+    for k in range(32):
+        s = 0.0
+        for t in terms[k * c:(k + 1) * c]:
+            s += t
+        parts.append(s)
+    total = parts[0]
+    for p in parts[1:]:
+        total += p
+    seq = 0.0
+    for t in terms:
+        seq += t
+    assert col[0] == 0
+    assert np.float64(val[0]).view(np.uint64) == np.float64(total).view(np.uint64)
+    assert total != seq  # the case does tell the two orders apart
+    # entries of one contribution are the product itself
+    assert np.array_equal(val[1:], b[2][1::2])
+
+
+def test_oracle_blocked_long_entry_f32():
+    """The same rule for FP32 Dot2 states: blocks folded with the Dot2 step, block states
+    combined by TwoSum of the sums plus the sum of the compensations."""
+    a, b, n = _long_entry_case()
+    f = np.float32
+    a32 = (a[0], a[1], a[2].astype(f))
+    b32 = (b[0], b[1], b[2].astype(f))
+    _, col, val = oracle.spgemm(*a32, *b32, n, dtype=np.float32)
+
+    def step(st, h):  # a = 1: TwoProduct is exact (r = 0)
+        s0, c0 = st
+        s = f(s0 + h)
+        z = f(s - s0)
+        q = f(f(s0 - f(s - z)) + f(h - z))
+        return s, f(c0 + f(q + f(0.0)))
+
+    def merge(u, v):
+        s = f(u[0] + v[0])
+        z = f(s - u[0])
+        q = f(f(u[0] - f(s - z)) + f(v[0] - z))
+        return s, f(f(u[1] + v[1]) + q)
+
+    terms = list(b32[2][0::2])
+    c = (len(terms) + 31) // 32
+    parts = []
+    for k in range(32):
+        st = (f(0.0), f(0.0))
+        for t in terms[k * c:(k + 1) * c]:
+            st = step(st, t)
+        parts.append(st)
+    tot = parts[0]
+    for p in parts[1:]:
+        tot = merge(tot, p)
+    want = f(tot[0] + tot[1])
+    assert col[0] == 0
+    assert np.float32(val[0]).view(np.uint32) == want.view(np.uint32)
