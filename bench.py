@@ -167,18 +167,21 @@ def _pair(data):
 
 
 def cpu_baseline(data, n, steps=3):
-    """Median time of the oracle's OpenMP port on the workload, its thread count, and its
-    result (the checker of the GPU result's parity)."""
+    """Median time of the oracle's OpenMP port on the workload, its thread count, and the
+    oracle's result (the checker of the GPU result's parity: the port keeps the plain
+    ascending-j fold for every entry, the oracle folds entries of more than 2,560 products
+    in blocks, as the library does)."""
     import oracle
 
     (ar, ac, av), (br, bc, bv) = _pair(data)
     av64, bv64 = np.asarray(av, dtype=np.float64), np.asarray(bv, dtype=np.float64)
-    ref = oracle.omp_spgemm(ar, ac, av64, br, bc, bv64)  # warm-up
+    oracle.omp_spgemm(ar, ac, av64, br, bc, bv64)  # warm-up
     ts = []
     for _ in range(steps):
         t0 = time.perf_counter()
         oracle.omp_spgemm(ar, ac, av64, br, bc, bv64)
         ts.append(time.perf_counter() - t0)
+    ref = oracle.spgemm(ar, ac, av64, br, bc, bv64, n)
     return statistics.median(ts), oracle.num_threads(), ref
 
 
@@ -198,7 +201,8 @@ def parity_report(gpu, ref, dt, scale_fn=None):
     same = (g_rpt.shape == o_rpt.shape and np.array_equal(g_rpt.astype(np.int64), o_rpt.astype(np.int64))
             and g_col.shape == o_col.shape and np.array_equal(g_col, o_col))
     tol = 1e-12 if dt == "f64" else 1e-5
-    rep = {"checked_against": "oracle (FP64, every entry folded in ascending j)", "structure_identical": bool(same),
+    rep = {"checked_against": "oracle (FP64, every entry folded in ascending j, in 32 blocks above 2,560 products)",
+           "structure_identical": bool(same),
            "tolerance_rel": tol}
     if not same:
         return rep
