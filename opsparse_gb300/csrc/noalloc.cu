@@ -24,7 +24,6 @@
 // host threads) race on it and must be serialized by the caller.  The call reads the total
 // back to the host and synchronizes its stream before it returns.
 #include <cstdint>
-#include <mutex>
 
 #include "common.cuh"
 #include "opsparse_gb300.h"
@@ -85,24 +84,14 @@ __global__ void __launch_bounds__(kNoAllocThreads) k_flop64_noalloc(const int *_
     }
 }
 
-std::mutex g_noalloc_mu;
-void *g_noalloc_addr[256] = {};  // device address of the scratch, per device ordinal
-
-// Device address of g_noalloc_scratch on the current device, looked up once per device.
+// Device address of g_noalloc_scratch on the current device, looked up on every call: an
+// address kept from an earlier call would be stale after a reset of the device's context.
 cudaError_t noalloc_scratch(NoAllocScratch **out)
 {
-    int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
+    void *p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
     if (e != cudaSuccess) return e;
-    if (dev < 0 || dev >= 256) return cudaErrorInvalidDevice;
-    std::lock_guard<std::mutex> lock(g_noalloc_mu);
-    if (!g_noalloc_addr[dev]) {
-        void *p = nullptr;
-        e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (e != cudaSuccess) return e;
-        g_noalloc_addr[dev] = p;
-    }
-    *out = static_cast<NoAllocScratch *>(g_noalloc_addr[dev]);
+    *out = static_cast<NoAllocScratch *>(p);
     return cudaSuccess;
 }
 
