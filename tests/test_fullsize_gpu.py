@@ -12,7 +12,7 @@ checked against the oracle on the same inputs, and its measured error is reporte
   C4  4,096 Erdos-Renyi problems (sizes log-uniform in 64..65,536, mean degree U(4,32)),
       FP32, one batch: every problem's result equals the single call's bit for bit (on the
       device), and a seeded sample of 48 problems matches the oracle as C3's FP32.
-Tolerances (the benchmark spec): FP64 1e-12 relative, FP32 1e-5 relative.
+Tolerances: FP64 1e-12 relative, FP32 1e-5 relative.
 """
 import numpy as np
 import pytest
