@@ -45,7 +45,7 @@ enum ops_status {
     OPS_INVALID_CSR = 7,       /* a column index outside [0, cols) or a malformed row_ptr */
     OPS_PROBE_LIMIT = 8,       /* an internal hash table overflowed (a library bug if seen) */
     OPS_TIMEOUT = 9,           /* a bounded device wait gave up */
-    OPS_NOT_SUPPORTED = 10,    /* no plan / request outside what this build supports */
+    OPS_NOT_SUPPORTED = 10,    /* no plan / request outside what the library supports */
     OPS_COUNT_MISMATCH = 11    /* numeric found a different nnz than symbolic (library bug) */
 };
 

@@ -1,7 +1,7 @@
 """OpSparse's own SpGEMM kernels run on the CPU (oracle/ref_emul, built into oracle/_ref/)
 — TEST INFRASTRUCTURE ONLY, used to pin the oracle and to generate golden fixtures.
 
-Available only where the OpSparse sources are (this build container); the GPU tests use
+Available only on a machine that holds the OpSparse sources; the GPU tests use
 the committed fixtures in tests/golden/ instead.
 """
 from __future__ import annotations

@@ -1,7 +1,7 @@
 """OpSparse's own SpGEMM kernels run on the GPU — TEST AND BENCHMARK INFRASTRUCTURE ONLY.
 
 The kernels are compiled from OpSparse's sources into oracle/_ref/ref_kernels.cubin by
-oracle/ref_gpu/Makefile (where the sources are, this build container); the cubin travels
+oracle/ref_gpu/Makefile on a machine that holds the sources; the cubin travels
 with the repository.  oracle/ref_gpu/ref_gpu.cu, built on the GPU machine, loads it and
 replays OpSparse's host sequence (phases, streams, allocations, synchronisations).  The
 GPU tests use it to check this library against the reference on the same GPU, and

@@ -1,7 +1,7 @@
 """Two-rank runs on the CPU (gloo): the multi-process paths of bench.py without a GPU.
 
 The library runs one process per GPU with replicas only (rows of C shard with no exchange
-but a scan of per-shard counts, and no run of this build has more than one GPU), so the
+but a scan of per-shard counts, and the runs here have one GPU each), so the
 multi-rank logic under test is the bench's: a torchrun launch whose reference arm runs on
 rank 0 alone, and the max-over-ranks reduction of a per-rank time.
 """
