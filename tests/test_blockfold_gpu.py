@@ -17,11 +17,12 @@ pytestmark = pytest.mark.gpu
 
 
 def long_entry_case(seed=41):
-    """A: 4 rows of 3,000, 4,100, 9,000 and 40 entries; each A entry owns a B row of 2-4
-    columns: a hub column (0, 1 or 2, chosen so the hubs collect thousands of products)
-    plus distinct private columns."""
+    """A: 5 rows of 3,000, 4,100, 9,000, 40 and 2,600 entries; each A entry owns a B row of
+    2-4 columns: hub columns (0, 1 or 2, chosen so the hubs collect thousands of products;
+    in the last row one hub of 2,561 and one of 2,560 products, either side of the rule's
+    bound) plus distinct private columns."""
     rng = np.random.default_rng(seed)
-    lens = [3000, 4100, 9000, 40]
+    lens = [3000, 4100, 9000, 40, 2600]
     b_rows = []
     nxt = 3
     for i, L in enumerate(lens):
@@ -29,6 +30,8 @@ def long_entry_case(seed=41):
             hubs = [0] if i != 1 else ([0, 1] if e % 3 else [1])
             if i == 2 and e % 2:
                 hubs = [0, 2]
+            if i == 4:  # column 0: 2,561 products (blocked); column 1: 2,560 (plain)
+                hubs = ([0] if e < 2561 else []) + ([1] if e < 2560 else [])
             priv = list(range(nxt, nxt + int(rng.integers(1, 3))))
             nxt += len(priv)
             b_rows.append(sorted(hubs + priv))
@@ -68,4 +71,4 @@ def test_long_entries_fold_in_blocks(cuda, dtype, oneshot, path):
     assert np.array_equal(col, ocol)
     bits = np.uint64 if dtype == "f64" else np.uint32
     assert np.array_equal(val.view(bits), oval.view(bits))
-    assert sub[path] >= 3, sub  # the three long rows took the path under test
+    assert sub[path] >= 4, sub  # the four long rows took the path under test

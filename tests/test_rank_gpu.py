@@ -44,7 +44,7 @@ def _row_b_rows(rng, kind, span):
 def rank_case(seed=5, wide=False):
     """A: 40 rows per group; row i owns B rows [24 i, 24 i + 24).  Narrow groups (B of
     65,536 columns, so every row fits the window): products in distinct columns (80 rows),
-    20, 50 and 100 late products (40 rows each) and crowded columns (40 rows).  wide=True:
+    20, 50, 100, 128 and 129 late products (40 rows each) and crowded columns (40 rows).  wide=True:
     40 rows of distinct columns spread over 200,000 columns (B wider than the window: the
     sort-only shape)."""
     rng = np.random.default_rng(seed)
@@ -52,7 +52,7 @@ def rank_case(seed=5, wide=False):
         kinds, ncols = [("distinct", 200000)], 200000
     else:
         kinds = [("distinct", 60000), ("late20", 60000), ("late50", 50000), ("late100", 65536), ("crowded", 30000),
-                 ("distinct", 2000)]
+                 ("distinct", 2000), ("late128", 60000), ("late129", 60000)]
         ncols = 65536
     b_rows = []
     for kind, span in kinds:
@@ -95,5 +95,6 @@ def test_rank_path_branches(cuda, dtype, oneshot, wide):
     if wide:
         assert sub["rank"] == 0 and sub["rank_refold"] == 0 and sub["rank_sorted"] == 0, sub
     else:
-        # 80 rows without late products, 120 re-folded, 40 sorted
-        assert sub["rank"] == 80 and sub["rank_refold"] == 120 and sub["rank_sorted"] == 40, sub
+        # 80 rows without late products, 160 re-folded (128 late products is the list's
+        # capacity), 80 sorted (crowded columns, and 129 late products)
+        assert sub["rank"] == 80 and sub["rank_refold"] == 160 and sub["rank_sorted"] == 80, sub
